@@ -1,0 +1,305 @@
+"""Benchmark: forward + exact adjoint gradients of the 4th-order C-PML acoustic solver.
+
+Workload (one "step"): the misfit gradient of a batch of 256 mixed-family 70 x 70 velocity models
+(10 m cells, pml 20 -> 114 x 114 padded), 5 surface shots at cells 0/17/34/52/69, 70 receivers,
+15 Hz Ricker, dt = 1 ms, nt = 1000, wavefield checkpoints every 50 steps with recomputation.
+Observed data come from the true models; the gradient is taken at their 5-cell Gaussian-smoothed
+versions. Data are synthetic (seeded), in the shapes and value ranges of the reference's setting.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints one JSON line (rank 0). `value` = gradients/s with inputs resident in HBM; `e2e` = the same
+through the C ABI's host entry point (host->device copy of velocities and observed data and
+device->host copy of losses and gradients inside the timed region).
+"""
+
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "gradients/s (forward + exact adjoint, 70x70, 5 shots, nt=1000)"
+UNIT = "gradients/s"
+MODELS = 256
+SHOTS = 5
+NT = 1000
+DT = 0.001
+NX = 70
+PML = 20
+CK = 50
+UPDATED_CELLS = (NX + 2 * (PML + 2) - 4) ** 2  # 110 x 110 cells updated per step
+FLOPS_PER_CELL_UPDATE = 48.0  # average over interior / one-PML-axis / two-PML-axes cells at pml 20
+
+
+def clocks_sampler(stop: threading.Event, out: list):
+    q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+    try:
+        p = subprocess.Popen(["nvidia-smi", f"--query-gpu={q}", "--format=csv,noheader,nounits", "-lms", "200"],
+                             stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+    except Exception:
+        return
+    dev = os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0]
+    try:
+        while not stop.is_set():
+            line = p.stdout.readline()
+            if not line:
+                break
+            out.append([x.strip() for x in line.split(",")])
+    finally:
+        p.terminate()
+
+
+def summarize_clocks(rows):
+    if not rows:
+        return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+    sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+    mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+    names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+    reasons = sorted({names[i] for r in rows for i in range(4) if len(r) > 5 + i and r[5 + i] == "Active"})
+    return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+            "reasons": reasons, "samples": len(rows)}
+
+
+def workload(models: int, seed: int = 0):
+    from wgnet_gb300 import models_synth
+
+    true = models_synth.make_batch(models, seed)
+    start = models_synth.smooth(true, 5.0)
+    src = np.stack([np.float32([0, 17, 34, 52, 69]) * np.float32(10.0), np.full(5, 10.0, np.float32)], 1)
+    return true, start, src.astype(np.float32)
+
+
+def measured_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def cpu_baseline(start, obs, src, cores: int, sample_models: int):
+    from oracle import native as o
+
+    sv = o.Survey(shots=SHOTS, nt=NT, dt=DT, pml=PML)
+    wav = o.ricker(NT, DT, 15.0)
+    m = sample_models
+    t0 = time.perf_counter()
+    o.gradients_parallel(sv, start[:m], src, wav, obs[:m], threads=cores)
+    dt = time.perf_counter() - t0
+    return m / dt, dt
+
+
+def run_reference(args):
+    """The reference's CPU solver path (C++ restatement of geology-core + the engine's adjoint;
+    the Rust crate itself cannot be built here) on all host cores."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    from oracle import native as o
+
+    cores = o.cpu_threads()
+    sample = max(cores, 1)
+    true, start, src = workload(sample)
+    sv = o.Survey(shots=SHOTS, nt=NT, dt=DT, pml=PML)
+    wav = o.ricker(NT, DT, 15.0)
+    obs = o.forward(sv, true, src, wav, threads=cores)
+    for _ in range(args.warmup):
+        o.gradients_parallel(sv, start[:sample], src, wav, obs[:sample], threads=cores)
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        o.gradients_parallel(sv, start[:sample], src, wav, obs[:sample], threads=cores)
+        times.append(time.perf_counter() - t0)
+    tot = sum(times)
+    value = sample * args.steps / tot
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * tot / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"{sample} mixed-family 70x70 models x 5 shots, nt=1000, dt=1ms (bounded sample of the "
+                               f"256-model batch)", "models_per_step": sample},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": f"{sample} gradients per step, one model per thread"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--models", type=int, default=MODELS)
+    ap.add_argument("--checkpoint", type=int, default=CK)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+
+    from wgnet_gb300 import _lib
+    from wgnet_gb300.engine import WaveEngine
+
+    lib = _lib.load()
+    M = args.models
+    true, start, src = workload(M, seed=rank)
+    eng = WaveEngine(shots=SHOTS, nt=NT, dt=DT, peak_hz=15.0, pml=PML, vmin=1000.0, vmax=5000.0,
+                     checkpoint_every=args.checkpoint)
+    eng.set_sources(src)
+    dev = torch.device("cuda", local)
+    d_true = torch.from_numpy(true).to(dev)
+    d_obs = eng.simulate_torch(d_true)
+    d_start = torch.from_numpy(start).to(dev)
+    torch.cuda.synchronize()
+
+    def step():
+        return eng.evaluate_adjoint_torch(d_start, d_obs)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+
+    # timed region: device-resident inputs
+    stop = threading.Event()
+    clk = []
+    th = threading.Thread(target=clocks_sampler, args=(stop, clk), daemon=True)
+    th.start()
+    time.sleep(0.3)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    lib.wg_profile(eng._h, 1)
+    _lib.launch_count(reset=True)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record()
+    for _ in range(args.steps):
+        loss, grad = step()
+    ev1.record()
+    torch.cuda.synchronize()
+    launches = _lib.launch_count()
+    ms = ev0.elapsed_time(ev1)
+    kms = (ctypes.c_double * 4)()
+    kn = (ctypes.c_longlong * 4)()
+    lib.wg_profile_read(eng._h, kms, kn, 4)
+    lib.wg_profile(eng._h, 0)
+    stop.set()
+    th.join(timeout=2)
+    if dist:
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * M * args.steps / (ms / 1000.0)
+    ms_step = ms / args.steps
+    assert torch.isfinite(loss).all() and torch.isfinite(grad).all()
+
+    # e2e: host pinned buffers through the C ABI's host entry point
+    h_vel = torch.from_numpy(start).pin_memory()
+    h_obs = d_obs.cpu().pin_memory()
+    h_loss = torch.empty(M, dtype=torch.float64).pin_memory()
+    h_grad = torch.empty((M, NX, NX), dtype=torch.float32).pin_memory()
+
+    def host_step():
+        _lib.check(lib.wg_evaluate_adjoint(eng._h, h_vel.data_ptr(), h_obs.data_ptr(), M, h_loss.data_ptr(),
+                                           h_grad.data_ptr()))
+
+    host_step()
+    if dist:
+        dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        host_step()
+    e2e_s = time.perf_counter() - t0
+    if dist:
+        t = torch.tensor([e2e_s], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e = world * M * args.steps / e2e_s
+    h2d = h_vel.numel() * 4 + h_obs.numel() * 4
+    d2h = h_loss.numel() * 8 + h_grad.numel() * 4
+
+    # roofline of the dominant kernel (live CUDA-event timings of every launch in the timed region)
+    names = ["forward", "recompute", "adjoint", "aux"]
+    dom = max(range(3), key=lambda k: kms[k])
+    units = M * SHOTS
+    seg = args.checkpoint if 0 < args.checkpoint < NT else NT
+    steps_per_launch = {0: NT, 1: seg, 2: seg}[dom]
+    cells_padded = (NX + 2 * (PML + 2)) ** 2
+    # algorithmic HBM bytes per launch of the dominant kernel
+    if dom == 2:  # adjoint: read stored terms of every updated cell and step, residuals; state in/out
+        per = units * steps_per_launch * (UPDATED_CELLS * 4 + 70 * 4)
+    elif dom == 1:  # recompute: write stored terms
+        per = units * steps_per_launch * UPDATED_CELLS * 4
+    else:  # forward: traces
+        per = units * NT * 70 * 4
+    avg_ms = kms[dom] / max(kn[dom], 1)
+    hbm_peak, peak_kind = measured_peaks()
+    achieved = per / (avg_ms / 1000.0) / 1e9
+    flops_launch = units * steps_per_launch * UPDATED_CELLS * FLOPS_PER_CELL_UPDATE
+    fp32_tflops = flops_launch / (avg_ms / 1000.0) / 1e12
+    cells_per_s = M * SHOTS * NT * UPDATED_CELLS * 2 / (ms_step / 1000.0)
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded mixed-family models: flat, curved, faulted, blob inclusions)",
+        "config": {"workload": f"config 3 gradient batch: {M} mixed-family 70x70 models x 5 shots, nt=1000, dt=1ms, "
+                               f"pml 20, checkpoint every {args.checkpoint} steps", "models_per_step": M,
+                   "shots": SHOTS, "nt": NT, "checkpoint_every": args.checkpoint,
+                   "l2": "inputs larger than L2 (observed 358 MB, checkpoints ~10 GB per step)",
+                   "launch_shape": {"forward": eng.launch_shape("forward"), "adjoint": eng.launch_shape("adjoint")}},
+        "gcell_updates_per_s": cells_per_s / 1e9,
+        "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "gpu_launches": launches,
+        "kernels_ms": {names[k]: {"total_ms": kms[k], "launches": int(kn[k])} for k in range(3)},
+        "roofline": {"kernel": names[dom], "bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                     "frac": achieved / hbm_peak, "traffic": None, "peak_source": peak_kind,
+                     "bytes_per_launch": per, "avg_launch_ms": avg_ms},
+        "roofline_fp32": {"kernel": names[dom], "achieved_tflops": fp32_tflops,
+                          "flops_per_launch": flops_launch, "flops_per_cell_update": FLOPS_PER_CELL_UPDATE},
+    }
+    line["clocks"] = summarize_clocks(clk)
+    if rank == 0 and not args.no_cpu_baseline:
+        from oracle import native as o
+
+        cores = o.cpu_threads()
+        v, secs = cpu_baseline(start, d_obs[: 2 * cores].cpu().numpy(), src, cores, 2 * cores)
+        line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+                                "sample": f"{2 * cores} of the {M} gradients ({secs:.1f} s), one model per thread"}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,130 @@
+/*
+ * wgnet_gb300 C ABI: the GB300 (sm_103a) wave engine behind WGNet's `wave_gauss_rs` interface.
+ *
+ * Plain C: opaque handles, plain pointers and sizes, int status codes (0 = success). On failure
+ * `wg_last_error()` returns a message for the calling thread. Entry points ending in `_dev` take
+ * device pointers and a cudaStream_t (passed as void*, NULL = the engine's own stream); the others
+ * take host pointers and block until their results are on the host.
+ *
+ * Each declaration names the reference interface it replaces (file:line in arthifact/WGNet).
+ */
+#ifndef WGNET_GB300_H
+#define WGNET_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes. */
+#define WG_OK 0
+#define WG_ERR_ARG 1          /* bad argument, shape or length (reference: PyValueError) */
+#define WG_ERR_CUDA 2         /* CUDA runtime error or no usable GPU */
+#define WG_ERR_NONFINITE 3    /* non-finite input */
+#define WG_ERR_ENERGY 4       /* observed traces have zero energy (reference: wave_wgpu.rs:853 panic) */
+#define WG_ERR_UNSUPPORTED 5  /* grid too large for the resident kernels */
+#define WG_ERR_CFL 6
+#define WG_ERR_OOM 7          /* device allocation failed */
+
+/* Engine configuration: the arguments of PyWaveEngine(shots, nt, dt, peak_hz, pml, vmin, vmax)
+ * (crates/wave-gauss-rs/src/lib.rs:51-57), plus the visible grid and spacing that the reference
+ * hard-wires (crates/geology-core/src/lib.rs:5-9: 70 x 70, 10 m). Zero in nx_vis/nz_vis/h/nrec
+ * selects the reference's value (70, 70, 10 m, one receiver per surface cell). */
+typedef struct wg_config {
+  int shots;
+  int nt;
+  float dt;
+  float peak_hz;
+  int pml;
+  float vmin;
+  float vmax;
+  int nx_vis;
+  int nz_vis;
+  float h;
+  int nrec;
+} wg_config;
+
+typedef struct wg_engine wg_engine;
+
+/* NativeWaveEngine::new (crates/wave-gauss-rs/src/wave_wgpu.rs:144-712): geometry (bilinear
+ * source/receiver corners, receiver CSR), C-PML profiles, Ricker wavelet, device statics. */
+int wg_engine_create(const wg_config* cfg, wg_engine** out);
+void wg_engine_destroy(wg_engine* eng);
+
+/* Read-only properties `shots`, `nt`, `nrec` (lib.rs:59-72) and the padded grid. */
+int wg_engine_dims(const wg_engine* eng, int* shots, int* nt, int* nrec, int* nx, int* nz, int* nx_vis,
+                   int* nz_vis);
+
+/* PyWaveEngine.sources / set_sources: [shots][2] (x, z) in metres (lib.rs:74-90,
+ * wave_wgpu.rs:761-785). `n` must equal shots. */
+int wg_get_sources(const wg_engine* eng, float* out, int n);
+int wg_set_sources(wg_engine* eng, const float* xz, int n);
+
+/* PyWaveEngine.wavelet / set_wavelet: [nt] (lib.rs:92-106, wave_wgpu.rs:788-795). */
+int wg_get_wavelet(const wg_engine* eng, float* out, int n);
+int wg_set_wavelet(wg_engine* eng, const float* w, int n);
+
+/* PyWaveEngine.simulate (lib.rs:108-116, wave_wgpu.rs:799-844) for `models` velocity models
+ * [models][nz_vis][nx_vis] in m/s -> traces [models][shots][nt][nrec]. */
+int wg_simulate(wg_engine* eng, const float* vel_mps, int models, float* traces);
+int wg_simulate_dev(wg_engine* eng, const float* d_vel_mps, int models, float* d_traces, void* stream);
+
+/* PyWaveEngine.evaluate_adjoint (lib.rs:118-137, wave_wgpu.rs:848-988) for `models` models:
+ * observed [models][shots][nt][nrec]; loss[m] = 0.5 |p - d|^2 / |d|^2 (f64), grad [models][nz_vis]
+ * [nx_vis] = dloss/d(v in m/s), zero where v is clamped, folded onto the visible grid. */
+int wg_evaluate_adjoint(wg_engine* eng, const float* vel_mps, const float* observed, int models, double* loss,
+                        float* grad);
+int wg_evaluate_adjoint_dev(wg_engine* eng, const float* d_vel_mps, const float* d_observed, int models,
+                            double* d_loss, float* d_grad, void* stream);
+
+/* Wavefield checkpoint interval for evaluate_adjoint: snapshots every k steps, segments recomputed
+ * in reverse. k <= 0 or k >= nt stores the gradient term of every step (the reference's scheme,
+ * wave_wgpu.rs:181-182). No reference counterpart for k > 0. */
+int wg_set_checkpoint_interval(wg_engine* eng, int k);
+int wg_get_checkpoint_interval(const wg_engine* eng);
+
+/* Launch shape of the resident kernels (which = 0 forward, 1 adjoint): CTAs per (model, shot)
+ * cluster, threads per CTA, cells-per-thread bound. wg_shape_candidates lists the compiled
+ * shapes that fit this engine's grid. No reference counterpart (wgpu dispatches 16x16 tiles). */
+int wg_set_launch_shape(wg_engine* eng, int which, int cluster, int threads, int cpt);
+int wg_get_launch_shape(const wg_engine* eng, int which, int* cluster, int* threads, int* cpt);
+int wg_shape_candidates(const wg_engine* eng, int which, int* out3, int max_shapes);
+
+/* geology_core::simulate_shot_cpu via PyO3 (crates/wave-gauss-rs/src/lib.rs:17-42,
+ * crates/geology-core/src/lib.rs:70-221): one shot, receivers at every surface node, d2 scaled by
+ * rh*rh precomputed as in the CPU solver. Runs on the GPU; out [nt][nx_vis]. */
+int wg_simulate_shot(const float* vel_mps, int nx_vis, int nz_vis, float h, float dt, int nt, int pml, float vmin,
+                     float vmax, float peak_hz, float src_x, float src_z, float* out);
+
+/* geology_core::ricker_wavelet (lib.rs:11-21) and cpml_profiles (lib.rs:23-68), host side. */
+int wg_ricker_wavelet(int samples, float dt, float peak_hz, float* out);
+int wg_cpml_profiles(int n, float h, float dt, int width, float max_vel, float freq, float* a, float* b, float* db);
+
+/* WavePhysics.bandlimit (python/wgnet/physics.py:48-57): causal FIR of `klen` taps along time for
+ * `series` blocks of [nt][nrec] traces, zero history before t = 0. Device pointers. */
+int wg_bandlimit_dev(const float* d_in, const float* d_kernel, int klen, int series, int nt, int nrec, float* d_out,
+                     void* stream);
+
+/* render_residual (python/wgnet/render.py:86-109): activated slot parameters [B][1225][6] ->
+ * residual field [B][70][70] in km/s; and its vector-Jacobian product: cotangent [B][70][70] ->
+ * parameter gradient [B][1225][6]. Device pointers. */
+int wg_render_fwd_dev(const float* d_params, int batch, float* d_field, void* stream);
+int wg_render_bwd_dev(const float* d_params, const float* d_cot, int batch, float* d_grad, void* stream);
+
+/* Per-kernel timing with CUDA events on the launching stream. wg_profile(eng, 1) starts
+ * recording (and clears earlier records); wg_profile_read fills ms[k] and launches[k] for kinds
+ * k = 0 forward (with receivers), 1 forward recompute (stored terms), 2 adjoint, and clears.
+ * No reference counterpart (wgpu timestamp_writes are off in the reference). */
+int wg_profile(wg_engine* eng, int enable);
+int wg_profile_read(wg_engine* eng, double* ms, long long* launches, int kinds);
+
+/* Message of the last failing call on this thread ("" if none). */
+const char* wg_last_error(void);
+
+/* Number of kernel launches this library issued on this thread since the last reset. */
+long long wg_launch_count(int reset);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* WGNET_GB300_H */

@@ -1,0 +1,212 @@
+"""The CPU oracle against the reference's known-answer tests, golden fixtures generated from the
+reference's Python, and an independent numpy restatement of the WGSL shaders. No GPU needed."""
+
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from conftest import ROOT, layered_model, rel_l2
+from oracle import native as o
+from oracle import physics_np, refine_np, render_np, wgsl_np
+
+GOLD = ROOT / "tests" / "golden"
+
+
+# --- crates/geology-core/src/lib.rs:227-251 -----------------------------------------------------
+
+def test_ricker_peak_and_cpml_profile():
+    w = o.ricker(2001, 0.0005, 15.0)
+    assert abs(w[200] - 1.0) < 1e-6  # peak at t = 1.5 / 15 Hz = 0.1 s
+    assert abs(w[0]) < 1e-3
+    a, b, db = o.cpml_profiles(114, 10.0, 0.0005, 20, 5000.0, 15.0)
+    assert a[55] == 0.0 and b[55] == 0.0
+    assert a[5] > 0.0 and b[5] < 0.0
+
+
+def test_cpu_wave_solver_propagates_and_stays_finite():
+    v = np.full(4900, 2500.0, np.float32)
+    tr = o.simulate_shot_cpu(v, 10.0, 0.0005, 400, 20, 1000.0, 5000.0, 15.0, 340.0, 10.0)
+    assert float(np.sum(tr.astype(np.float64) ** 2)) > 1e-4
+    assert np.isfinite(tr).all()
+
+
+# --- crates/wave-gauss-rs/src/wave_wgpu.rs:1023-1054: engine forward vs CPU solver --------------
+
+def test_engine_forward_matches_cpu_solver_two_layer():
+    vel = np.full((70, 70), 2500.0, np.float32)
+    vel[35:] = 3200.0
+    sv = o.Survey(shots=5, nt=2001)
+    eng = o.forward(sv, vel, sv.default_sources(), o.ricker(2001, 0.0005, 15.0))
+    cpu0 = o.simulate_shot_cpu(vel, 10.0, 0.0005, 2001, 20, 1000.0, 5000.0, 15.0, 0.0, 10.0)
+    assert 100.0 * rel_l2(eng[0, 0], cpu0) < 0.05  # the reference's bound, in percent
+    # the two differ only in rounding (d2 * rh * rh vs d2 * rh2)
+    assert rel_l2(eng[0, 0], cpu0) < 1e-5
+
+
+def test_default_sources_match_reference_layout():
+    src = o.Survey(shots=5).default_sources()
+    np.testing.assert_array_equal(src[:, 0], np.float32([0.0, 172.5, 345.0, 517.5, 690.0]))
+    assert (src[:, 1] == 10.0).all()
+    one = o.Survey(shots=1).default_sources()
+    assert one[0, 0] == np.float32(345.0)
+
+
+# --- two independent restatements agree bit for bit ----------------------------------------------
+
+def _small_case(seed=0, shots=3, nt=150, nxv=20, nzv=16, pml=6):
+    rng = np.random.default_rng(seed)
+    vel = (2000 + 1500 * rng.random((nzv, nxv))).astype(np.float32)
+    vel[0, 0] = 900.0      # clamped low (vmin = 1000)
+    vel[3, 4] = 5200.0     # clamped high (vmax = 5000)
+    src = np.array([[0.0, 10.0], [95.0, 10.0], [190.0, 12.5]], np.float32)[:shots]
+    sv = o.Survey(shots=shots, nt=nt, dt=0.001, nx_vis=nxv, nz_vis=nzv, pml=pml)
+    return sv, vel, src, o.ricker(nt, 0.001, 15.0)
+
+
+def test_cpp_oracle_equals_numpy_wgsl_restatement_forward():
+    sv, vel, src, wav = _small_case()
+    geo = wgsl_np.Geometry(sv.nx_vis, sv.nz_vis, sv.pml, sv.h, sv.dt, sv.peak_hz, sv.vmin, sv.vmax, src)
+    trn, stn = wgsl_np.forward(geo, vel, wav, store=True)
+    trc, stc = o.forward(sv, vel, src, wav, store=True)
+    np.testing.assert_array_equal(trn, trc[0])
+    np.testing.assert_array_equal(stn, stc[0])
+
+
+def test_cpp_oracle_equals_numpy_wgsl_restatement_adjoint():
+    sv, vel, src, wav = _small_case(seed=3)
+    geo = wgsl_np.Geometry(sv.nx_vis, sv.nz_vis, sv.pml, sv.h, sv.dt, sv.peak_hz, sv.vmin, sv.vmax, src)
+    obs = o.forward(sv, vel * np.float32(1.04), src, wav)
+    ln, gn, rawn = wgsl_np.evaluate_adjoint(geo, vel, wav, obs[0])
+    lc, gc, rawc = o.evaluate_adjoint(sv, vel, src, wav, obs, raw=True)
+    np.testing.assert_array_equal(rawn, rawc[0])
+    np.testing.assert_array_equal(gn, gc[0])
+    assert abs(ln - lc[0]) <= 1e-12 * abs(lc[0])
+
+
+def test_cpml_and_ricker_restatements_agree():
+    for n, w in ((114, 20), (184, 20), (40, 6)):
+        for a, b in zip(o.cpml_profiles(n, 10.0, 0.001, w, 5000.0, 15.0), wgsl_np.cpml(n, 10.0, 0.001, w, 5000.0, 15.0)):
+            np.testing.assert_array_equal(a, b)
+    # numpy's vectorised exp may differ from libm expf in the last place
+    np.testing.assert_allclose(o.ricker(1000, 0.001, 15.0), wgsl_np.ricker(1000, 0.001, 15.0), rtol=0, atol=2e-7)
+
+
+# --- the adjoint is the exact derivative: FP64 finite differences --------------------------------
+
+def test_adjoint_matches_fp64_finite_differences():
+    sv, vel, src, wav = _small_case(seed=5, nt=250)
+    vel = np.clip(vel, 1500, 4500).astype(np.float32)  # keep away from the clamp
+    obs = o.forward(sv, vel * np.float32(1.03), src, wav)
+    rng = np.random.default_rng(9)
+    direction = rng.standard_normal(vel.shape).astype(np.float32)
+    _, g64 = o.evaluate_adjoint(sv, vel, src, wav, obs, precision="f64")
+    eps = 1e-3  # m/s; FD on the FP64 run
+    lp, _ = o.evaluate_adjoint(sv, (vel.astype(np.float64) + eps * direction).astype(np.float32), src, wav, obs,
+                               precision="f64")
+    lm, _ = o.evaluate_adjoint(sv, (vel.astype(np.float64) - eps * direction).astype(np.float32), src, wav, obs,
+                               precision="f64")
+    # the perturbed velocities are rounded to f32; use the actual f32 perturbation
+    dv = ((vel.astype(np.float64) + eps * direction).astype(np.float32).astype(np.float64)
+          - (vel.astype(np.float64) - eps * direction).astype(np.float32).astype(np.float64))
+    fd = (lp[0] - lm[0])
+    adj = float(np.sum(g64[0] * dv))
+    assert abs(fd - adj) <= 1e-5 * abs(fd), (fd, adj)
+
+
+def test_fp32_gradient_close_to_fp64():
+    sv, vel, src, wav = _small_case(seed=8, nt=200)
+    obs = o.forward(sv, vel * np.float32(1.05), src, wav)
+    l32, g32 = o.evaluate_adjoint(sv, vel, src, wav, obs)
+    l64, g64 = o.evaluate_adjoint(sv, vel, src, wav, obs, precision="f64")
+    assert rel_l2(g32, g64) < 1e-4
+    assert abs(l32[0] - l64[0]) < 1e-4 * l64[0]
+
+
+def test_clamped_cells_have_zero_gradient():
+    sv, vel, src, wav = _small_case(seed=1)
+    obs = o.forward(sv, vel * np.float32(1.02), src, wav)
+    _, g = o.evaluate_adjoint(sv, vel, src, wav, obs)
+    assert g[0, 0, 0] == 0.0 and g[0, 3, 4] == 0.0
+    assert np.count_nonzero(g) > 0.9 * g.size
+
+
+def test_zero_energy_is_an_error():
+    sv, vel, src, wav = _small_case()
+    with pytest.raises(ValueError):
+        o.evaluate_adjoint(sv, vel, src, wav, np.zeros((1, sv.shots, sv.nt, sv.n_receivers), np.float32))
+
+
+def test_geometry_csr_and_corners():
+    sv = o.Survey(shots=2, nt=10)
+    geo = o.geometry(sv, np.array([[0.0, 10.0], [172.5, 17.5]], np.float32))
+    # receivers on nodes: one non-zero corner each, all on row pad + 1
+    assert geo["n_entries"] == 70
+    assert geo["csr"][-1] == 70
+    nz_w = geo["rec_w"].reshape(70, 4)
+    assert (nz_w[:, 0] == 1.0).all() and (nz_w[:, 1:] == 0.0).all()
+    w = geo["src_w"].reshape(2, 4)
+    np.testing.assert_array_equal(w[0], np.float32([1, 0, 0, 0]))
+    # (172.5, 17.5) m -> gx = 39.25, gz = 23.75: fx = 0.25, fz = 0.75
+    np.testing.assert_array_equal(w[1], np.float32([0.75 * 0.25, 0.25 * 0.25, 0.75 * 0.75, 0.25 * 0.75]))
+    assert geo["src_cell"][4] == 23 * 114 + 39
+
+
+# --- golden fixtures from the reference's Python --------------------------------------------------
+
+def test_renderer_oracle_matches_reference_golden():
+    g = np.load(GOLD / "render.npz")
+    np.testing.assert_allclose(render_np.render(g["params"]), g["field"], rtol=0, atol=1e-12)
+    v = render_np.render_vjp(g["params"], g["cot"])
+    np.testing.assert_allclose(v, g["grad"], rtol=1e-10, atol=1e-12)
+
+
+def test_renderer_vjp_matches_finite_differences():
+    # python/verify.py:42-54 (fd vs adjoint, tolerance 1e-5) on the oracle
+    g = np.load(GOLD / "render.npz")
+    params = g["params"][:1]
+    cot = g["cot"][:1]
+    rng = np.random.default_rng(1)
+    d = rng.standard_normal(params.shape) * np.array([0.3, 0.3, 0.1, 0.1, 0.1, 0.1])
+    eps = 1e-4
+    fd = (np.sum(render_np.render(params + eps * d) * cot) - np.sum(render_np.render(params - eps * d) * cot)) / (2 * eps)
+    adj = float(np.sum(render_np.render_vjp(params, cot) * d))
+    assert abs(fd - adj) / max(abs(fd), 1e-9) < 1e-5
+
+
+def test_band_schedule_oracle_matches_reference_golden():
+    p = np.load(GOLD / "physics.npz")
+    for k in p.files:
+        if k.startswith("lowpass_"):
+            _, dt, f = k.split("_")
+            np.testing.assert_array_equal(physics_np.lowpass_kernel(float(f), float(dt)), p[k])
+    for f in (6.0, 12.0):
+        y = physics_np.bandlimit(p["bandlimit_in"], physics_np.lowpass_kernel(f, 0.001))
+        np.testing.assert_allclose(y, p[f"bandlimit_{f}"], rtol=0, atol=1e-6)
+    for f in (6.0, 9.0, 12.0):
+        np.testing.assert_array_equal(physics_np.band_wavelet(p["setband_full"], physics_np.lowpass_kernel(f, 0.001)),
+                                      p[f"setband_{f}"])
+
+
+def test_lbfgs_direction_matches_reference_golden():
+    r = np.load(GOLD / "refine.npz")
+    for c in range(4):
+        s, y = list(r[f"s_{c}"]), list(r[f"y_{c}"])
+        rho = [1.0 / float(np.dot(a, b)) for a, b in zip(s, y)]
+        np.testing.assert_array_equal(refine_np.lbfgs_direction(r[f"grad_{c}"], s, y, rho), r[f"dir_{c}"])
+
+
+def test_band_identity_on_oracle():
+    # python/verify.py:76-84: synthetics of the low-passed wavelet == low-passed synthetics
+    sv, vel, src, wav = _small_case(nt=300)
+    k = physics_np.lowpass_kernel(8.0, sv.dt)
+    low = o.forward(sv, vel, src, physics_np.band_wavelet(wav, k))
+    full = o.forward(sv, vel, src, wav)
+    filt = physics_np.bandlimit(full, k)
+    assert float(np.abs(low - filt).max() / np.abs(filt).max()) < 2e-3
+
+
+def test_layered_model_generator():
+    v = layered_model(0)
+    assert v.shape == (70, 70) and v.min() >= 1500 and v.max() <= 4500
+    assert (np.diff(v[:, 0]) >= 0).all()

@@ -1,0 +1,11 @@
+// Explicit instantiations of the resident kernels for some launch shapes (see wave_table.cu).
+#include "wave_kernels.cuh"
+
+namespace wg {
+
+template <>
+cudaError_t fwd_dispatch<1, 1024, 12>(bool traces, bool store, const FwdArgs& a, size_t smem, cudaStream_t s) {
+  return fwd_dispatch_impl<1, 1024, 12>(traces, store, a, smem, s);
+}
+
+}  // namespace wg

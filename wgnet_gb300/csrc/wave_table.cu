@@ -1,0 +1,88 @@
+#include <cuda_runtime.h>
+
+#include "wave_device.cuh"
+#include "wave_launch.h"
+
+// Launch table of the resident kernels. The kernel templates live in wave_kernels.cuh; each
+// compiled shape is instantiated in one of the wave_inst_*.cu files so that they build in parallel.
+
+namespace wg {
+
+#define WG_SHAPES(X) \
+  X(1, 1024, 12)     \
+  X(2, 1024, 6)      \
+  X(2, 512, 12)      \
+  X(2, 1024, 10)     \
+  X(2, 1024, 16)     \
+  X(4, 1024, 8)      \
+  X(4, 512, 16)
+
+#define WG_ADJ_SHAPES(X) \
+  X(2, 1024, 6)          \
+  X(2, 512, 12)          \
+  X(4, 1024, 4)          \
+  X(4, 1024, 8)          \
+  X(4, 512, 16)
+
+
+// Compiled launch shapes. A shape is usable for a grid when its cells-per-thread bound covers the
+// CTA's rows and its shared-memory layout fits the 227 KB per-CTA limit.
+#define WG_LIST(Cc, NTt, CPTt) {Cc, NTt, CPTt},
+static const Shape kFwdShapes[] = {WG_SHAPES(WG_LIST)};
+static const Shape kAdjShapes[] = {WG_ADJ_SHAPES(WG_LIST)};
+#undef WG_LIST
+
+int fwd_shape_count() { return static_cast<int>(sizeof(kFwdShapes) / sizeof(kFwdShapes[0])); }
+int adj_shape_count() { return static_cast<int>(sizeof(kAdjShapes) / sizeof(kAdjShapes[0])); }
+Shape fwd_shape(int i) { return kFwdShapes[i]; }
+Shape adj_shape(int i) { return kAdjShapes[i]; }
+
+size_t fwd_smem_bytes(const Shape& s, int nx, int nz, int sw, int nrec) {
+  return static_cast<size_t>(fwd_layout(nx, nz, sw, s.cluster, nrec).total) * sizeof(float);
+}
+size_t adj_smem_bytes(const Shape& s, int nx, int nz, int swa) {
+  return static_cast<size_t>(adj_layout(nx, nz, swa, s.cluster).total) * sizeof(float);
+}
+
+bool fwd_shape_fits(const Shape& s, int nx, int nz, int sw, int nrec) {
+  if (nx < 2 * sw || nz < 2 * sw) return false;  // left/right (top/bottom) strips must not overlap
+  const int rows = max_rows(nz, s.cluster);
+  if (static_cast<long>(rows) * (nx - 2 * FD_PAD) > static_cast<long>(s.threads) * s.cpt) return false;
+  if (fwd_smem_bytes(s, nx, nz, sw, nrec) > kMaxSmemPerCta) return false;
+  if (s.cluster > 1) {
+    // Each z strip (sw rows) must be updated and read inside the first / last CTA.
+    if (split_row(nz, s.cluster, 1) < sw || split_row(nz, s.cluster, s.cluster - 1) > nz - sw) return false;
+  }
+  return nx < 65536 && nz < 32768;
+}
+
+bool adj_shape_fits(const Shape& s, int nx, int nz, int swa) {
+  if (nx < 2 * swa || nz < 2 * swa) return false;
+  const int rows = max_rows(nz, s.cluster);
+  if (static_cast<long>(rows) * (nx - 2 * FD_PAD) > static_cast<long>(s.threads) * s.cpt) return false;
+  if (adj_smem_bytes(s, nx, nz, swa) > kMaxSmemPerCta) return false;
+  if (s.cluster > 1) {
+    if (split_row(nz, s.cluster, 1) < swa || split_row(nz, s.cluster, s.cluster - 1) > nz - swa) return false;
+  }
+  return nx < 65536 && nz < 32768;
+}
+
+cudaError_t launch_fwd(const Shape& s, bool traces, bool store, const FwdArgs& a, cudaStream_t stream) {
+  const size_t smem = fwd_smem_bytes(s, a.g.nx, a.g.nz, a.g.sw, a.st.nrec);
+#define WG_FWD(Cc, NTt, CPTt) \
+  if (s.cluster == Cc && s.threads == NTt && s.cpt == CPTt) return fwd_dispatch<Cc, NTt, CPTt>(traces, store, a, smem, stream);
+  WG_SHAPES(WG_FWD)
+#undef WG_FWD
+  return cudaErrorInvalidValue;
+}
+
+cudaError_t launch_adj(const Shape& s, const AdjArgs& a, cudaStream_t stream) {
+  const size_t smem = adj_smem_bytes(s, a.g.nx, a.g.nz, a.g.swa);
+#define WG_ADJ(Cc, NTt, CPTt) \
+  if (s.cluster == Cc && s.threads == NTt && s.cpt == CPTt) return adj_dispatch<Cc, NTt, CPTt>(a, smem, stream);
+  WG_ADJ_SHAPES(WG_ADJ)
+#undef WG_ADJ
+  return cudaErrorInvalidValue;
+}
+
+}  // namespace wg
