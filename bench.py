@@ -149,10 +149,12 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--models", type=int, default=MODELS)
     ap.add_argument("--checkpoint", type=int, default=CK)
+    ap.add_argument("--nt", type=int, default=NT, help="time steps (profiling runs use a short record)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    nt = args.nt
 
     import torch
 
@@ -172,7 +174,7 @@ def main():
     lib = _lib.load()
     M = args.models
     true, start, src = workload(M, seed=rank)
-    eng = WaveEngine(shots=SHOTS, nt=NT, dt=DT, peak_hz=15.0, pml=PML, vmin=1000.0, vmax=5000.0,
+    eng = WaveEngine(shots=SHOTS, nt=nt, dt=DT, peak_hz=15.0, pml=PML, vmin=1000.0, vmax=5000.0,
                      checkpoint_every=args.checkpoint)
     eng.set_sources(src)
     dev = torch.device("cuda", local)
@@ -250,8 +252,8 @@ def main():
     names = ["forward", "recompute", "adjoint", "aux"]
     dom = max(range(3), key=lambda k: kms[k])
     units = M * SHOTS
-    seg = args.checkpoint if 0 < args.checkpoint < NT else NT
-    steps_per_launch = {0: NT, 1: seg, 2: seg}[dom]
+    seg = args.checkpoint if 0 < args.checkpoint < nt else nt
+    steps_per_launch = {0: nt, 1: seg, 2: seg}[dom]
     cells_padded = (NX + 2 * (PML + 2)) ** 2
     # algorithmic HBM bytes per launch of the dominant kernel
     if dom == 2:  # adjoint: read stored terms of every updated cell and step, residuals; state in/out
@@ -259,21 +261,21 @@ def main():
     elif dom == 1:  # recompute: write stored terms
         per = units * steps_per_launch * UPDATED_CELLS * 4
     else:  # forward: traces
-        per = units * NT * 70 * 4
+        per = units * nt * 70 * 4
     avg_ms = kms[dom] / max(kn[dom], 1)
     hbm_peak, peak_kind = measured_peaks()
     achieved = per / (avg_ms / 1000.0) / 1e9
     flops_launch = units * steps_per_launch * UPDATED_CELLS * FLOPS_PER_CELL_UPDATE
     fp32_tflops = flops_launch / (avg_ms / 1000.0) / 1e12
-    cells_per_s = M * SHOTS * NT * UPDATED_CELLS * 2 / (ms_step / 1000.0)
+    cells_per_s = M * SHOTS * nt * UPDATED_CELLS * 2 / (ms_step / 1000.0)
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded mixed-family models: flat, curved, faulted, blob inclusions)",
-        "config": {"workload": f"config 3 gradient batch: {M} mixed-family 70x70 models x 5 shots, nt=1000, dt=1ms, "
+        "config": {"workload": f"config 3 gradient batch: {M} mixed-family 70x70 models x 5 shots, nt={nt}, dt=1ms, "
                                f"pml 20, checkpoint every {args.checkpoint} steps", "models_per_step": M,
-                   "shots": SHOTS, "nt": NT, "checkpoint_every": args.checkpoint,
+                   "shots": SHOTS, "nt": nt, "checkpoint_every": args.checkpoint,
                    "l2": "inputs larger than L2 (observed 358 MB, checkpoints ~10 GB per step)",
                    "launch_shape": {"forward": eng.launch_shape("forward"), "adjoint": eng.launch_shape("adjoint")}},
         "gcell_updates_per_s": cells_per_s / 1e9,

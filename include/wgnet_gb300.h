@@ -3,8 +3,9 @@
  *
  * Plain C: opaque handles, plain pointers and sizes, int status codes (0 = success). On failure
  * `wg_last_error()` returns a message for the calling thread. Entry points ending in `_dev` take
- * device pointers and a cudaStream_t (passed as void*, NULL = the engine's own stream); the others
- * take host pointers and block until their results are on the host.
+ * device pointers and a cudaStream_t (passed as void*; NULL = the CUDA default stream) and are
+ * asynchronous on that stream; the others take host pointers, run on the engine's own stream and
+ * block until their results are on the host.
  *
  * Each declaration names the reference interface it replaces (file:line in arthifact/WGNet).
  */

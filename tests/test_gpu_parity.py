@@ -211,7 +211,11 @@ def test_dropin_engine_api(cuda_lib):
     assert isinstance(loss, float) and g.shape == (70, 70)
     w = e.wavelet()
     e.set_wavelet(w * np.float32(2.0))
-    np.testing.assert_allclose(e.simulate(v), 2 * tr, rtol=1e-5, atol=1e-9)
+    tr2 = e.simulate(v)
+    # linear in the wavelet up to f32 rounding (the oracle shows the same last-place deviations)
+    np.testing.assert_allclose(tr2, 2 * tr, rtol=1e-4, atol=1e-9)
+    sv = o.Survey(shots=2, nt=300, dt=0.001)
+    np.testing.assert_array_equal(tr2, o.forward(sv, v.reshape(70, 70), e.sources(), w * np.float32(2.0))[0])
     e.set_sources(np.float32([[100, 20], [300, 30]]))
     np.testing.assert_array_equal(e.sources(), np.float32([[100, 20], [300, 30]]))
 

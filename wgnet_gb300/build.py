@@ -26,8 +26,10 @@ INCLUDE = ROOT / "include"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # -fmad=false: no contraction of a*b+c, so every f32 operation rounds as in the reference.
+# -Xcompiler -ffp-contract=off: the same for host code (g++ contracts by default on aarch64), so the
+# host-side wavelet and C-PML profiles are identical on x86_64 and aarch64.
 NVCC_FLAGS = ["-O3", "-std=c++17", "-fmad=false", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
-              "--expt-relaxed-constexpr"]
+              "-Xcompiler", "-ffp-contract=off", "--expt-relaxed-constexpr"]
 
 
 def nvcc() -> str:
@@ -45,6 +47,11 @@ def build(force: bool = False, verbose: bool = False) -> Path:
     sources = sorted(CSRC.glob("*.cu"))
     BUILD.mkdir(exist_ok=True)
     OUT_DIR.mkdir(exist_ok=True)
+    stamp = BUILD / "flags.txt"
+    flags = " ".join([*ARCH, *NVCC_FLAGS, os.uname().machine])
+    if not stamp.exists() or stamp.read_text() != flags:
+        force = True
+        stamp.write_text(flags)
     hdr_mtime = max((h.stat().st_mtime for h in _headers()), default=0.0)
     jobs = []
     objs = []

@@ -358,7 +358,9 @@ int create_impl(const wg_config* c, bool cpu_d2, wg_engine** out) {
   return WG_OK;
 }
 
-cudaStream_t pick_stream(wg_engine* e, void* s) { return s ? static_cast<cudaStream_t>(s) : e->stream; }
+// Device entry points run on the caller's stream; NULL is the CUDA default stream (torch's
+// default stream has handle 0).
+cudaStream_t pick_stream(wg_engine*, void* s) { return static_cast<cudaStream_t>(s); }
 
 // Kernel kinds for per-kernel timing.
 enum : int { K_FWD = 0, K_RECOMPUTE = 1, K_ADJ = 2, K_AUX = 3, K_KINDS = 4 };

@@ -468,7 +468,7 @@ __global__ void __launch_bounds__(NT, 1) adj_kernel(const __grid_constant__ AdjA
           const float v = vel[cell];
 #pragma unroll
           for (int k = 0; k < 4; ++k)
-            if (cell == sc[k]) gt = gt + (lc[m] * ((((-2.0f) * v) * dt2) * p.st.src_w[4 * shot + k]) * f);
+            if (cell == sc[k]) gt = gt + lc[m] * (((((-2.0f) * v) * dt2) * p.st.src_w[4 * shot + k]) * f);
         }
         ga[m] = ga[m] + gt;
         lp[m] = lc[m];
