@@ -118,6 +118,18 @@ int wg_render_bwd_dev(const float* d_params, const float* d_cot, int batch, floa
 int wg_profile(wg_engine* eng, int enable);
 int wg_profile_read(wg_engine* eng, double* ms, long long* launches, int kinds);
 
+/* evaluate_adjoint that allocates nothing: no counterpart in the reference. For callers that
+ * cannot call cudaMalloc at call time because another allocator owns the GPU's memory (a
+ * framework's caching allocator that reserved the device, a service with a fixed memory budget).
+ * Same inputs and outputs as wg_evaluate_adjoint_dev (device pointers, caller's stream); all
+ * intermediates live in one static 48 MiB device array that the library holds on every GPU that
+ * loads it until the process exits. Sizes needing more scratch (about 35 MiB per 70x70 5-shot
+ * model at nt = 1000) are rejected with WG_ERR_ARG. The first call on a device looks up the
+ * array's address (make that call before any stream capture). Calls share the array: calls that
+ * overlap on the GPU (other streams, other threads) race and corrupt each other's results. */
+int wg_evaluate_adjoint_noalloc(wg_engine* eng, const float* d_vel_mps, const float* d_observed, int models,
+                                double* d_loss, float* d_grad, void* stream);
+
 /* Message of the last failing call on this thread ("" if none). */
 const char* wg_last_error(void);
 

@@ -61,6 +61,7 @@ SIGNATURES: dict[str, tuple] = {
     "wg_render_bwd_dev": (_I, [_P, _P, _I, _P, _P]),
     "wg_profile": (_I, [_P, _I]),
     "wg_profile_read": (_I, [_P, _P, _P, _I]),
+    "wg_evaluate_adjoint_noalloc": (_I, [_P, _P, _P, _I, _P, _P, _P]),
     "wg_last_error": (ctypes.c_char_p, []),
     "wg_launch_count": (ctypes.c_longlong, [_I]),
 }

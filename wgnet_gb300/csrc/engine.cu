@@ -543,6 +543,36 @@ int read_status(wg_engine* e) {
 
 }  // namespace
 
+namespace wg {
+
+// Snapshot of the engine's statics under its lock; `lock` keeps the engine locked while the caller
+// launches with them.
+EngineView engine_view(wg_engine* e, std::unique_lock<std::mutex>& lock) {
+  lock = std::unique_lock<std::mutex>(e->mu);
+  EngineView v;
+  v.grid = e->grid();
+  v.stations = e->stations();
+  v.shots = e->shots;
+  v.nt = e->nt;
+  v.nrec = e->nrec;
+  v.nx = e->nx;
+  v.nz = e->nz;
+  v.nx_vis = e->nx_vis;
+  v.nz_vis = e->nz_vis;
+  v.pad = e->pad;
+  v.ck_every = e->ck_every;
+  v.vmin = e->cfg.vmin;
+  v.vmax = e->cfg.vmax;
+  v.fshape = e->fshape;
+  v.ashape = e->ashape;
+  v.d_status = e->d_status.as<int>();
+  return v;
+}
+
+int engine_device(const wg_engine* e) { return e->device; }
+
+}  // namespace wg
+
 extern "C" {
 
 int wg_engine_create(const wg_config* cfg, wg_engine** out) { return create_impl(cfg, false, out); }

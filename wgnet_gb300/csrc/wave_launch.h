@@ -60,6 +60,17 @@ cudaError_t launch_bandlimit(const float* in, const float* ker, int klen, int se
 int report_error(int code, const char* msg);
 void note_launch();
 
+// Read-only view of an engine's device statics and launch settings, for entry points that
+// sequence the kernels with their own buffers.
+struct EngineView {
+  Grid grid;
+  Stations stations;
+  int shots, nt, nrec, nx, nz, nx_vis, nz_vis, pad, ck_every;
+  float vmin, vmax;
+  Shape fshape, ashape;
+  int* d_status;
+};
+
 // out[i] = in[i] * alpha (unit conversion), n elements.
 cudaError_t launch_scale(const float* in, float alpha, size_t n, float* out, cudaStream_t s);
 
