@@ -260,3 +260,35 @@ def test_waveloss_autograd(cuda_lib):
     (3.0 * loss.sum()).backward()
     _, g = eng.evaluate_adjoint((f.detach() * 1000.0).cpu().numpy(), obs)
     np.testing.assert_allclose(f.grad.cpu().numpy(), 3.0 * 1000.0 * g, rtol=1e-6)
+
+
+def test_every_forward_shape_bitexact_70x70(cuda_lib):
+    """Each compiled forward launch shape that fits 70x70 (both kernel generations)."""
+    sv = o.Survey(shots=3, nt=260, dt=0.001)
+    src = np.float32([[0.0, 10.0], [333.3, 10.0], [685.0, 47.5]])
+    eng = make_engine(sv, src)
+    wav = eng.wavelet()
+    vel = np.stack([layered_model(21), layered_model(22)])
+    vel[1, 30:40, 5:60] = 900.0  # clamped patch
+    ref = o.forward(sv, vel, src, wav)
+    shapes = eng.shape_candidates("forward")
+    assert len(shapes) >= 3
+    for shape in shapes:
+        eng.set_launch_shape("forward", shape)
+        np.testing.assert_array_equal(eng.simulate(vel), ref, err_msg=f"shape {shape}")
+
+
+@pytest.mark.parametrize("k", [0, 37])
+def test_gradient_with_every_forward_shape_70x70(cuda_lib, k):
+    sv = o.Survey(shots=2, nt=240, dt=0.001)
+    src = np.float32([[120.0, 10.0], [545.5, 12.0]])
+    eng = make_engine(sv, src, checkpoint_every=k)
+    wav = eng.wavelet()
+    cur = layered_model(31)
+    obs = o.forward(sv, layered_model(32), src, wav)
+    rl, rg = o.evaluate_adjoint(sv, cur, src, wav, obs)
+    for shape in eng.shape_candidates("forward"):
+        eng.set_launch_shape("forward", shape)
+        loss, grad = eng.evaluate_adjoint(cur, obs)
+        np.testing.assert_array_equal(grad, rg, err_msg=f"shape {shape}")
+        np.testing.assert_allclose(loss, rl, rtol=1e-12)

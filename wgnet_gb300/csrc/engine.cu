@@ -263,22 +263,42 @@ int set_receivers_impl(wg_engine* e) {
   return WG_OK;
 }
 
+// Compiled shape with this (cluster, threads, cells-per-thread) triple.
+bool find_shape(int which, int cluster, int threads, int cpt, wg::Shape* out) {
+  const int n = which == 0 ? wg::fwd_shape_count() : wg::adj_shape_count();
+  for (int i = 0; i < n; ++i) {
+    const wg::Shape k = which == 0 ? wg::fwd_shape(i) : wg::adj_shape(i);
+    if (k.cluster == cluster && k.threads == threads && k.cpt == cpt) {
+      *out = k;
+      return true;
+    }
+  }
+  return false;
+}
+
 bool pick_shapes(wg_engine* e) {
-  static const wg::Shape fpref[] = {{2, 1024, 6}, {1, 1024, 12}, {2, 512, 12}, {2, 1024, 10},
-                                    {4, 1024, 8}, {2, 1024, 16}, {4, 512, 16}};
-  static const wg::Shape apref[] = {{2, 1024, 6}, {2, 512, 12}, {4, 1024, 4}, {4, 1024, 8}, {4, 512, 16}};
-  e->fshape = {0, 0, 0};
-  e->ashape = {0, 0, 0};
-  for (const auto& s : fpref)
-    if (wg::fwd_shape_fits(s, e->nx, e->nz, e->sw, e->nrec)) {
+  // Preference order; the first compiled shape that fits the grid is the default (the autotuner
+  // can choose another among wg_shape_candidates).
+  static const int fpref[][3] = {{2, 448, 16}, {4, 448, 8}, {4, 896, 4}, {4, 672, 10}, {4, 864, 10},
+                                 {2, 1024, 6}, {1, 1024, 12}, {2, 512, 12}, {2, 1024, 10},
+                                 {4, 1024, 8}, {2, 1024, 16}, {4, 512, 16}};
+  static const int apref[][3] = {{2, 1024, 6}, {2, 512, 12}, {4, 1024, 4}, {4, 1024, 8}, {4, 512, 16}};
+  e->fshape = wg::Shape{0, 0, 0};
+  e->ashape = wg::Shape{0, 0, 0};
+  for (const auto& t : fpref) {
+    wg::Shape s;
+    if (find_shape(0, t[0], t[1], t[2], &s) && wg::fwd_shape_fits(s, e->nx, e->nz, e->sw, e->nrec)) {
       e->fshape = s;
       break;
     }
-  for (const auto& s : apref)
-    if (wg::adj_shape_fits(s, e->nx, e->nz, e->swa)) {
+  }
+  for (const auto& t : apref) {
+    wg::Shape s;
+    if (find_shape(1, t[0], t[1], t[2], &s) && wg::adj_shape_fits(s, e->nx, e->nz, e->swa)) {
       e->ashape = s;
       break;
     }
+  }
   return e->fshape.cluster > 0;
 }
 
@@ -728,28 +748,16 @@ int wg_get_checkpoint_interval(const wg_engine* e) { return e ? e->ck_every : -1
 
 int wg_set_launch_shape(wg_engine* e, int which, int cluster, int threads, int cpt) {
   if (!e) return fail(WG_ERR_ARG, "null engine");
-  const wg::Shape s{cluster, threads, cpt};
+  if (which != 0 && which != 1) return fail(WG_ERR_ARG, "which must be 0 (forward) or 1 (adjoint)");
+  wg::Shape s;
+  if (!find_shape(which, cluster, threads, cpt, &s)) return fail(WG_ERR_ARG, "launch shape not compiled");
   std::lock_guard<std::mutex> lk(e->mu);
   if (which == 0) {
-    bool known = false;
-    for (int i = 0; i < wg::fwd_shape_count(); ++i) {
-      const wg::Shape k = wg::fwd_shape(i);
-      known |= k.cluster == cluster && k.threads == threads && k.cpt == cpt;
-    }
-    if (!known || !wg::fwd_shape_fits(s, e->nx, e->nz, e->sw, e->nrec))
-      return fail(WG_ERR_ARG, "forward shape not compiled or does not fit this grid");
+    if (!wg::fwd_shape_fits(s, e->nx, e->nz, e->sw, e->nrec)) return fail(WG_ERR_ARG, "forward shape does not fit this grid");
     e->fshape = s;
-  } else if (which == 1) {
-    bool known = false;
-    for (int i = 0; i < wg::adj_shape_count(); ++i) {
-      const wg::Shape k = wg::adj_shape(i);
-      known |= k.cluster == cluster && k.threads == threads && k.cpt == cpt;
-    }
-    if (!known || !wg::adj_shape_fits(s, e->nx, e->nz, e->swa))
-      return fail(WG_ERR_ARG, "adjoint shape not compiled or does not fit this grid");
-    e->ashape = s;
   } else {
-    return fail(WG_ERR_ARG, "which must be 0 (forward) or 1 (adjoint)");
+    if (!wg::adj_shape_fits(s, e->nx, e->nz, e->swa)) return fail(WG_ERR_ARG, "adjoint shape does not fit this grid");
+    e->ashape = s;
   }
   return WG_OK;
 }

@@ -1,6 +1,7 @@
 #include <cuda_runtime.h>
 
 #include "wave_device.cuh"
+#include "wave_kernels2_layout.h"
 #include "wave_launch.h"
 
 // Launch table of the resident kernels. The kernel templates live in wave_kernels.cuh; each
@@ -17,6 +18,16 @@ namespace wg {
   X(4, 1024, 8)      \
   X(4, 512, 16)
 
+// generation-2 forward shapes: (C, S rows per segment, segments, interior warps per segment)
+#define WG_FWD2_SHAPES(X) \
+  X(2, 4, 14, 1)          \
+  X(2, 8, 7, 1)           \
+  X(1, 8, 14, 1)          \
+  X(4, 4, 7, 1)           \
+  X(4, 2, 14, 1)          \
+  X(4, 5, 7, 2)           \
+  X(4, 5, 9, 2)
+
 #define WG_ADJ_SHAPES(X) \
   X(2, 1024, 6)          \
   X(2, 512, 12)          \
@@ -27,10 +38,12 @@ namespace wg {
 
 // Compiled launch shapes. A shape is usable for a grid when its cells-per-thread bound covers the
 // CTA's rows and its shared-memory layout fits the 227 KB per-CTA limit.
-#define WG_LIST(Cc, NTt, CPTt) {Cc, NTt, CPTt},
-static const Shape kFwdShapes[] = {WG_SHAPES(WG_LIST)};
+#define WG_LIST(Cc, NTt, CPTt) Shape{Cc, NTt, CPTt, 1, 0, 0, 0},
+#define WG_LIST2(Cc, Ss, NSEGs, NIs) Shape{Cc, NSEGs * 32 * (1 + NIs), 2 * Ss, 2, Ss, NSEGs, NIs},
+static const Shape kFwdShapes[] = {WG_FWD2_SHAPES(WG_LIST2) WG_SHAPES(WG_LIST)};
 static const Shape kAdjShapes[] = {WG_ADJ_SHAPES(WG_LIST)};
 #undef WG_LIST
+#undef WG_LIST2
 
 int fwd_shape_count() { return static_cast<int>(sizeof(kFwdShapes) / sizeof(kFwdShapes[0])); }
 int adj_shape_count() { return static_cast<int>(sizeof(kAdjShapes) / sizeof(kAdjShapes[0])); }
@@ -38,6 +51,7 @@ Shape fwd_shape(int i) { return kFwdShapes[i]; }
 Shape adj_shape(int i) { return kAdjShapes[i]; }
 
 size_t fwd_smem_bytes(const Shape& s, int nx, int nz, int sw, int nrec) {
+  if (s.kind == 2) return static_cast<size_t>(fwd2_layout(nx, nz, sw, s.cluster, nrec).total) * sizeof(float);
   return static_cast<size_t>(fwd_layout(nx, nz, sw, s.cluster, nrec).total) * sizeof(float);
 }
 size_t adj_smem_bytes(const Shape& s, int nx, int nz, int swa) {
@@ -47,7 +61,15 @@ size_t adj_smem_bytes(const Shape& s, int nx, int nz, int swa) {
 bool fwd_shape_fits(const Shape& s, int nx, int nz, int sw, int nrec) {
   if (nx < 2 * sw || nz < 2 * sw) return false;  // left/right (top/bottom) strips must not overlap
   const int rows = max_rows(nz, s.cluster);
-  if (static_cast<long>(rows) * (nx - 2 * FD_PAD) > static_cast<long>(s.threads) * s.cpt) return false;
+  if (s.kind == 2) {
+    // column pairs: even width; the PML warp's 32 columns per side must cover the PML region;
+    // the interior warps must cover the columns in between
+    if ((nx & 1) || nx < 2 * kSwx + 4 || sw - 2 > kPmlCols + FD_PAD) return false;
+    if ((nx - 2 * FD_PAD - 2 * kPmlCols) / 2 > 32 * s.ni) return false;
+    if (rows > s.seg_rows * s.nseg) return false;
+  } else if (static_cast<long>(rows) * (nx - 2 * FD_PAD) > static_cast<long>(s.threads) * s.cpt) {
+    return false;
+  }
   if (fwd_smem_bytes(s, nx, nz, sw, nrec) > kMaxSmemPerCta) return false;
   if (s.cluster > 1) {
     // Each z strip (sw rows) must be updated and read inside the first / last CTA.
@@ -69,6 +91,14 @@ bool adj_shape_fits(const Shape& s, int nx, int nz, int swa) {
 
 cudaError_t launch_fwd(const Shape& s, bool traces, bool store, const FwdArgs& a, cudaStream_t stream) {
   const size_t smem = fwd_smem_bytes(s, a.g.nx, a.g.nz, a.g.sw, a.st.nrec);
+  if (s.kind == 2) {
+#define WG_FWD2(Cc, Ss, NSEGs, NIs)                                                          \
+  if (s.cluster == Cc && s.seg_rows == Ss && s.nseg == NSEGs && s.ni == NIs)                 \
+    return fwd2_dispatch<Cc, Ss, NSEGs, NIs>(traces, store, a, smem, stream);
+    WG_FWD2_SHAPES(WG_FWD2)
+#undef WG_FWD2
+    return cudaErrorInvalidValue;
+  }
 #define WG_FWD(Cc, NTt, CPTt) \
   if (s.cluster == Cc && s.threads == NTt && s.cpt == CPTt) return fwd_dispatch<Cc, NTt, CPTt>(traces, store, a, smem, stream);
   WG_SHAPES(WG_FWD)
