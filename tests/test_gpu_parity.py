@@ -292,3 +292,23 @@ def test_gradient_with_every_forward_shape_70x70(cuda_lib, k):
         loss, grad = eng.evaluate_adjoint(cur, obs)
         np.testing.assert_array_equal(grad, rg, err_msg=f"shape {shape}")
         np.testing.assert_allclose(loss, rl, rtol=1e-12)
+
+
+@pytest.mark.parametrize("k", [0, 45])
+def test_every_adjoint_shape_bitexact_70x70(cuda_lib, k):
+    """Each compiled adjoint launch shape that fits 70x70 (both kernel generations)."""
+    sv = o.Survey(shots=3, nt=220, dt=0.001)
+    src = np.float32([[0.0, 10.0], [351.5, 25.0], [690.0, 10.0]])
+    eng = make_engine(sv, src, checkpoint_every=k)
+    wav = eng.wavelet()
+    cur = np.stack([layered_model(41), layered_model(42)])
+    cur[0, 10:20, 30:50] = 5500.0  # clamped patch: zero gradient there
+    obs = o.forward(sv, np.stack([layered_model(43), layered_model(44)]), src, wav)
+    rl, rg = o.evaluate_adjoint(sv, cur, src, wav, obs)
+    shapes = eng.shape_candidates("adjoint")
+    assert len(shapes) >= 3
+    for shape in shapes:
+        eng.set_launch_shape("adjoint", shape)
+        loss, grad = eng.evaluate_adjoint(cur, obs)
+        np.testing.assert_array_equal(grad, rg, err_msg=f"shape {shape}")
+        np.testing.assert_allclose(loss, rl, rtol=1e-12)

@@ -279,10 +279,11 @@ bool find_shape(int which, int cluster, int threads, int cpt, wg::Shape* out) {
 bool pick_shapes(wg_engine* e) {
   // Preference order; the first compiled shape that fits the grid is the default (the autotuner
   // can choose another among wg_shape_candidates).
-  static const int fpref[][3] = {{2, 448, 16}, {4, 448, 8}, {4, 896, 4}, {4, 672, 10}, {4, 864, 10},
-                                 {2, 1024, 6}, {1, 1024, 12}, {2, 512, 12}, {2, 1024, 10},
-                                 {4, 1024, 8}, {2, 1024, 16}, {4, 512, 16}};
-  static const int apref[][3] = {{2, 1024, 6}, {2, 512, 12}, {4, 1024, 4}, {4, 1024, 8}, {4, 512, 16}};
+  static const int fpref[][3] = {{2, 896, 8}, {2, 704, 10}, {4, 896, 4}, {4, 448, 8}, {2, 1024, 6},
+                                 {1, 1024, 12}, {2, 512, 12}, {2, 1024, 10}, {4, 1024, 8}, {2, 1024, 16},
+                                 {4, 512, 16}};
+  static const int apref[][3] = {{4, 448, 8}, {4, 896, 4}, {2, 704, 10}, {2, 896, 8}, {2, 1024, 6},
+                                 {2, 512, 12}, {4, 1024, 4}, {4, 1024, 8}, {4, 512, 16}};
   e->fshape = wg::Shape{0, 0, 0};
   e->ashape = wg::Shape{0, 0, 0};
   for (const auto& t : fpref) {

@@ -111,13 +111,14 @@ enum Status : int {
   ST_OOM = 7,
 };
 
-// Kernel launch shape chosen per grid: kernel generation (1: flat cell mapping, 2: column-pair x
-// segment mapping), cluster size (CTAs per unit), threads per CTA and the static cells-per-thread
-// bound the kernel was compiled with. Generation 2 also fixes the segment length S (rows), the
+// Kernel launch shape chosen per grid: kernel generation (1: flat cell mapping, 3: column-pair x
+// segment mapping for a compile-time grid width), cluster size (CTAs per unit), threads per CTA and the static cells-per-thread
+// bound the kernel was compiled with. Generation 3 also fixes the segment length S (rows), the
 // number of segments and the number of interior warps per segment.
 struct Shape {
   int cluster, threads, cpt;
   int kind = 1, seg_rows = 0, nseg = 0, ni = 0;
+  int nxc = 0, pmlp = 0;  // generation 3: compile-time grid width and PML column pairs per side
 };
 
 }  // namespace wg

@@ -1,0 +1,688 @@
+// Third-generation resident kernels (forward and adjoint) for grids of compile-time width NX.
+//
+// Thread mapping: each thread owns a pair of adjacent columns (x, x+1) over a segment of S rows.
+// Per segment, one "PML warp" owns the PMLP leftmost and PMLP rightmost column pairs (exactly the
+// C-PML region of the adjoint, which contains the forward's) and runs the PML formulas; the
+// remaining "interior warps" own the pairs in between and run the interior formulas, so no warp
+// diverges on the PML test. With NX known at compile time every shared-memory access of a row is
+// a per-thread base register plus an immediate offset.
+//
+// Values a cell's neighbours read (the wavefield, a*psi, the adjoint's derived terms) are exchanged
+// through double-buffered shared memory (one barrier per step); a thread's own leapfrog pair stays
+// in registers, and the update writes the new value over the oldest one, alternating the roles of
+// the two register arrays every step. Arithmetic follows the reference's operation order (the
+// library is built with -fmad=false), so results are bit-identical to the f32 restatement.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "wave_device.cuh"
+#include "wave_kernels.cuh"
+#include "wave_kernels3_layout.h"
+#include "wave_launch.h"
+
+namespace wg {
+
+// Column layout of a generation-3 kernel.
+template <int NX, int PMLP>
+struct Cols3 {
+  static constexpr int PCOLS = 2 * PMLP;          // PML columns per side, starting at x = 2
+  static constexpr int SW = PCOLS + 4;            // packed strip width per side (reads reach x+3); = g3_sw
+  static constexpr int IPAIRS = (NX - 4 - 2 * PCOLS) / 2;
+  __device__ static int x_of(int wk, int lane) {
+    if (wk == 0) return lane < PMLP ? FD_PAD + 2 * lane : (NX - FD_PAD - PCOLS) + 2 * (lane - PMLP);
+    return FD_PAD + PCOLS + 2 * ((wk - 1) * 32 + lane);
+  }
+  __device__ static bool active(int wk, int lane) {
+    if (wk == 0) return lane < 2 * PMLP;
+    return (wk - 1) * 32 + lane < IPAIRS;
+  }
+  __host__ __device__ static int strip(int x) { return x < SW ? x : x - (NX - 2 * SW); }
+};
+
+__device__ __forceinline__ float2 lds2(const float* p) { return *reinterpret_cast<const float2*>(p); }
+__device__ __forceinline__ void sts2(float* p, float a, float b) { *reinterpret_cast<float2*>(p) = make_float2(a, b); }
+
+__device__ __forceinline__ void st_peer_v2(const float* local_ptr, unsigned peer, float a, float b) {
+  unsigned la = static_cast<unsigned>(__cvta_generic_to_shared(local_ptr));
+  unsigned ra;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(ra) : "r"(la), "r"(peer));
+  asm volatile("st.shared::cluster.v2.f32 [%0], {%1, %2};" ::"r"(ra), "f"(a), "f"(b) : "memory");
+}
+
+// ------------------------------------------------------------------------------------------------
+// Forward (splatForward.wgsl:48-121)
+// ------------------------------------------------------------------------------------------------
+template <int NX, int PMLP, int C, int S, int NSEG, int NI, bool TRACES, bool STORE>
+__global__ void __launch_bounds__(NSEG * 32 * (1 + NI), 1) fwd3_kernel(const __grid_constant__ FwdArgs p) {
+  using CL = Cols3<NX, PMLP>;
+  constexpr int SW = CL::SW;
+  constexpr int NT = NSEG * 32 * (1 + NI);
+  extern __shared__ __align__(16) float sm[];
+  const Grid& g = p.g;
+  const int nz = g.nz, sw = g.sw, region = g.region, nrec = p.st.nrec;
+  const float rh = g.rh, dt2 = g.dt2, d2a = g.d2a, d2b = g.d2b;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int seg = warp / (1 + NI), wk = warp % (1 + NI);
+  const int rank = (C > 1) ? static_cast<int>(cluster_rank()) : 0;
+  const int unit = blockIdx.x / C;
+  const int shot = unit % p.st.shots;
+  const int model = unit / p.st.shots;
+  const size_t cells = static_cast<size_t>(NX) * nz;
+  const F3Layout L = f3_layout_rt(NX, PMLP, nz, sw, C, nrec);
+  const int r0 = split_row(nz, C, rank), r1 = split_row(nz, C, rank + 1);
+  const int zl0 = r0 - FD_PAD;
+  const int bot_off = (C == 1) ? sw : 0;
+  const int ustride = L.lr * NX, xstride = L.maxrows * 2 * SW, zstride = L.zs * NX;
+  float* U = sm + L.off_u;
+  float* APX = sm + L.off_apx;
+  float* ZX = sm + L.off_zx;
+  float* APZ = sm + L.off_apz;
+  float* ZZ = sm + L.off_zz;
+  float* sAZ = sm + L.off_prof + 3 * NX;
+  float* sBZ = sAZ + nz;
+  float* sDBZ = sBZ + nz;
+  int* sRecCell = reinterpret_cast<int*>(sm + L.off_rec);
+  float* sRecW = sm + L.off_rec + 4 * nrec;
+  int* sRecOk = reinterpret_cast<int*>(sm + L.off_rec + 8 * nrec);
+
+  for (int i = tid; i < L.total; i += NT) sm[i] = 0.0f;
+  __syncthreads();
+  for (int i = tid; i < 3 * (NX + nz); i += NT) sm[L.off_prof + i] = g.prof[i];
+  if (TRACES) {
+    for (int r = tid; r < nrec; r += NT) {
+      const int z0 = p.st.rec_cell[4 * r] / NX;
+      const bool ok = (z0 >= r0 || rank == 0) && (z0 < r1 || rank == C - 1);
+      sRecOk[r] = ok ? 1 : 0;
+      for (int k = 0; k < 4; ++k) {
+        const int cell = p.st.rec_cell[4 * r + k];
+        sRecCell[4 * r + k] = ok ? (cell / NX - zl0) * NX + cell % NX : 0;
+        sRecW[4 * r + k] = p.st.rec_w[4 * r + k];
+      }
+    }
+  }
+
+  const bool pml = (wk == 0);
+  const int x = CL::x_of(wk, lane);
+  const int zb = r0 + seg * S;
+  const int nrows = CL::active(wk, lane) ? max(0, min(S, r1 - zb)) : 0;
+  const int ubase = (zb - zl0) * NX + x;                 // row 0 of the segment in U
+  const int abase = (zb - r0) * 2 * SW + CL::strip(x);   // row 0 in APX / ZX (PML warp)
+  const int zsh = (zb < nz / 2) ? 0 : (nz - sw - bot_off);
+  const int zbase = (zb - zsh) * NX + x;                 // row 0 in APZ / ZZ (z-strip rows)
+  const int gbase = zb * NX + x;                         // row 0 in a global [nz][NX] field
+
+  float ax0 = 0.f, ax1 = 0.f, bx0 = 0.f, bx1 = 0.f, dbx0 = 0.f, dbx1 = 0.f;
+  if (pml) {
+    ax0 = g.prof[x];
+    ax1 = g.prof[x + 1];
+    bx0 = g.prof[NX + x];
+    bx1 = g.prof[NX + x + 1];
+    dbx0 = g.prof[2 * NX + x];
+    dbx1 = g.prof[2 * NX + x + 1];
+  }
+  const float opbx0 = 1.0f + bx0, opbx1 = 1.0f + bx1;
+
+  float uA[S][2], uB[S][2];
+  unsigned srcmask = 0;
+  const int* sc = p.st.src_cell + 4 * shot;
+  const float* vel = p.vel + static_cast<size_t>(model) * cells + gbase;
+#pragma unroll
+  for (int i = 0; i < S; ++i) {
+    uA[i][0] = uA[i][1] = uB[i][0] = uB[i][1] = 0.f;
+    if (i < nrows) {
+      const int cell = gbase + i * NX;
+      if (cell == sc[0] || cell == sc[1] || cell == sc[2] || cell == sc[3]) srcmask |= 1u << (2 * i);
+      if (cell + 1 == sc[0] || cell + 1 == sc[1] || cell + 1 == sc[2] || cell + 1 == sc[3])
+        srcmask |= 1u << (2 * i + 1);
+    }
+  }
+
+  const size_t ckf = ckpt_floats(NX, nz, sw);
+  if (p.ck_in) {
+    const float* ck = p.ck_in + (static_cast<size_t>(unit) * p.ck_slots + p.ck_in_slot) * ckf;
+    const float* cU = ck;
+    const float* cP = ck + cells;
+    const float* cAX = ck + 2 * cells;
+    const float* cAZ = cAX + static_cast<size_t>(nz) * 2 * sw;
+    const float* cZX = cAZ + static_cast<size_t>(2) * sw * NX;
+    const float* cZZ = cZX + static_cast<size_t>(nz) * 2 * sw;
+    constexpr int W = NX - 2 * FD_PAD;
+    const int ra = max(r0 - FD_PAD, FD_PAD), rb = min(r1 + FD_PAD, nz - FD_PAD);
+    for (int i = tid; i < (rb - ra) * W; i += NT) {
+      const int z = ra + i / W, xx = FD_PAD + i % W;
+      U[(z - zl0) * NX + xx] = cU[z * NX + xx];
+    }
+#pragma unroll
+    for (int i = 0; i < S; ++i) {
+      if (i < nrows) {
+        const int z = zb + i;
+#pragma unroll
+        for (int j = 0; j < 2; ++j) {
+          const int xx = x + j;
+          uA[i][j] = cU[z * NX + xx];
+          uB[i][j] = cP[z * NX + xx];
+          if (xx < sw || xx >= NX - sw) {
+            const int xc = strip_col(xx, NX, sw);
+            APX[abase + i * 2 * SW + j] = cAX[z * 2 * sw + xc];
+            ZX[abase + i * 2 * SW + j] = cZX[z * 2 * sw + xc];
+          }
+          if (z < sw || z >= nz - sw) {
+            const int zc = strip_col(z, nz, sw);
+            APZ[zbase + i * NX + j] = cAZ[zc * NX + xx];
+            ZZ[zbase + i * NX + j] = cZZ[zc * NX + xx];
+          }
+        }
+      }
+    }
+  }
+  if constexpr (C > 1) cluster_barrier();
+  else __syncthreads();
+
+  const int pr_lo = (rank > 0) ? split_row(nz, C, rank - 1) - FD_PAD : 0;
+
+  auto step = [&](int t, float (&uc)[S][2], float (&un)[S][2]) {
+    const int par = (t - p.t0) & 1;
+    const float* Uc = U + par * ustride + ubase;
+    float* Un = U + (1 - par) * ustride + ubase;
+    const float* APXc = APX + par * xstride + abase;
+    float* APXn = APX + (1 - par) * xstride + abase;
+    float* ZXo = ZX + abase;
+    const float* APZc = APZ + par * zstride + zbase;
+    float* APZn = APZ + (1 - par) * zstride + zbase;
+    float* ZZo = ZZ + zbase;
+
+    if (TRACES) {
+      const float* Ucb = U + par * ustride;
+      for (int r = tid; r < nrec; r += NT) {
+        if (sRecOk[r]) {
+          float acc = 0.0f;
+#pragma unroll
+          for (int k = 0; k < 4; ++k) acc = acc + sRecW[4 * r + k] * Ucb[sRecCell[4 * r + k]];
+          p.traces[(static_cast<size_t>(unit) * g.nt + t) * nrec + r] = acc;
+        }
+      }
+    }
+    if (p.ck_out && t > p.t0 && (t % p.ck_every) == 0) {
+      float* ck = p.ck_out + (static_cast<size_t>(unit) * p.ck_slots + (t / p.ck_every - 1)) * ckf;
+      float* cAX = ck + 2 * cells;
+      float* cAZ = cAX + static_cast<size_t>(nz) * 2 * sw;
+      float* cZX = cAZ + static_cast<size_t>(2) * sw * NX;
+      float* cZZ = cZX + static_cast<size_t>(nz) * 2 * sw;
+#pragma unroll
+      for (int i = 0; i < S; ++i) {
+        if (i < nrows) {
+          const int z = zb + i;
+#pragma unroll
+          for (int j = 0; j < 2; ++j) {
+            const int xx = x + j;
+            ck[z * NX + xx] = uc[i][j];
+            ck[cells + z * NX + xx] = un[i][j];
+            if (xx < sw || xx >= NX - sw) {
+              const int xc = strip_col(xx, NX, sw);
+              cAX[z * 2 * sw + xc] = APXc[i * 2 * SW + j];
+              cZX[z * 2 * sw + xc] = ZXo[i * 2 * SW + j];
+            }
+            if (z < sw || z >= nz - sw) {
+              const int zc = strip_col(z, nz, sw);
+              cAZ[zc * NX + xx] = APZc[i * NX + j];
+              cZZ[zc * NX + xx] = ZZo[i * NX + j];
+            }
+          }
+        }
+      }
+    }
+
+    const float f = __ldg(&g.wavelet[t]);
+    float* st = STORE ? p.stored + (static_cast<size_t>(unit) * (p.t1 - p.t0) + (t - p.t0)) * cells + gbase : nullptr;
+#pragma unroll
+    for (int i = 0; i < S; ++i) {
+      if (i < nrows) {
+        const int z = zb + i;
+        const float2 A = lds2(Uc + i * NX - 2);
+        const float2 B = lds2(Uc + i * NX + 2);
+        float zm2[2], zm1[2], zp1[2], zp2[2];
+        if (i >= 2) {
+          zm2[0] = uc[i - 2][0];
+          zm2[1] = uc[i - 2][1];
+        } else {
+          const float2 q = lds2(Uc + (i - 2) * NX);
+          zm2[0] = q.x;
+          zm2[1] = q.y;
+        }
+        if (i >= 1) {
+          zm1[0] = uc[i - 1][0];
+          zm1[1] = uc[i - 1][1];
+        } else {
+          const float2 q = lds2(Uc + (i - 1) * NX);
+          zm1[0] = q.x;
+          zm1[1] = q.y;
+        }
+        if (i + 1 < S && i + 1 < nrows) {
+          zp1[0] = uc[i + 1 < S ? i + 1 : i][0];
+          zp1[1] = uc[i + 1 < S ? i + 1 : i][1];
+        } else {
+          const float2 q = lds2(Uc + (i + 1) * NX);
+          zp1[0] = q.x;
+          zp1[1] = q.y;
+        }
+        if (i + 2 < S && i + 2 < nrows) {
+          zp2[0] = uc[i + 2 < S ? i + 2 : i][0];
+          zp2[1] = uc[i + 2 < S ? i + 2 : i][1];
+        } else {
+          const float2 q = lds2(Uc + (i + 2) * NX);
+          zp2[0] = q.x;
+          zp2[1] = q.y;
+        }
+        const float u0 = uc[i][0], u1 = uc[i][1];
+        const float d2x0 = (((F_D2A * u0 + F_D2B * (u1 + A.y)) - F_D2C * (B.x + A.x)) * d2a) * d2b;
+        const float d2x1 = (((F_D2A * u1 + F_D2B * (B.x + u0)) - F_D2C * (B.y + A.y)) * d2a) * d2b;
+        float w0, w1;
+        if (pml) {
+          const float2 P0 = lds2(APXc + i * 2 * SW - 2);
+          const float2 P1 = lds2(APXc + i * 2 * SW);
+          const float2 P2 = lds2(APXc + i * 2 * SW + 2);
+          const float2 Z = lds2(ZXo + i * 2 * SW);
+          const float d10 = ((F_D1A * (u1 - A.y)) - F_D1B * (B.x - A.x)) * rh;
+          const float d11 = ((F_D1A * (B.x - u0)) - F_D1B * (B.y - A.y)) * rh;
+          const float da0 = ((F_D1A * (P1.y - P0.y)) - F_D1B * (P2.x - P0.x)) * rh;
+          const float da1 = ((F_D1A * (P2.x - P1.x)) - F_D1B * (P2.y - P0.y)) * rh;
+          const float tmp0 = ((opbx0 * d2x0) + (dbx0 * d10)) + da0;
+          const float tmp1 = ((opbx1 * d2x1) + (dbx1 * d11)) + da1;
+          w0 = (opbx0 * tmp0) + (ax0 * Z.x);
+          w1 = (opbx1 * tmp1) + (ax1 * Z.y);
+          const float psi0 = (bx0 * d10) + P1.x;
+          const float psi1 = (bx1 * d11) + P1.y;
+          sts2(ZXo + i * 2 * SW, (bx0 * tmp0) + (ax0 * Z.x), (bx1 * tmp1) + (ax1 * Z.y));
+          sts2(APXn + i * 2 * SW, ax0 * psi0, ax1 * psi1);
+        } else {
+          w0 = d2x0;
+          w1 = d2x1;
+        }
+        const float d2z0 = (((F_D2A * u0 + F_D2B * (zp1[0] + zm1[0])) - F_D2C * (zp2[0] + zm2[0])) * d2a) * d2b;
+        const float d2z1 = (((F_D2A * u1 + F_D2B * (zp1[1] + zm1[1])) - F_D2C * (zp2[1] + zm2[1])) * d2a) * d2b;
+        if (z < region || z >= nz - region) {
+          const float az = sAZ[z], bz = sBZ[z], dbz = sDBZ[z];
+          const float opbz = 1.0f + bz;
+          const float2 Qm2 = lds2(APZc + (i - 2) * NX);
+          const float2 Qm1 = lds2(APZc + (i - 1) * NX);
+          const float2 Q0 = lds2(APZc + i * NX);
+          const float2 Qp1 = lds2(APZc + (i + 1) * NX);
+          const float2 Qp2 = lds2(APZc + (i + 2) * NX);
+          const float2 Z = lds2(ZZo + i * NX);
+          const float d10 = ((F_D1A * (zp1[0] - zm1[0])) - F_D1B * (zp2[0] - zm2[0])) * rh;
+          const float d11 = ((F_D1A * (zp1[1] - zm1[1])) - F_D1B * (zp2[1] - zm2[1])) * rh;
+          const float da0 = ((F_D1A * (Qp1.x - Qm1.x)) - F_D1B * (Qp2.x - Qm2.x)) * rh;
+          const float da1 = ((F_D1A * (Qp1.y - Qm1.y)) - F_D1B * (Qp2.y - Qm2.y)) * rh;
+          const float tmp0 = ((opbz * d2z0) + (dbz * d10)) + da0;
+          const float tmp1 = ((opbz * d2z1) + (dbz * d11)) + da1;
+          w0 = w0 + ((opbz * tmp0) + (az * Z.x));
+          w1 = w1 + ((opbz * tmp1) + (az * Z.y));
+          const float psi0 = (bz * d10) + Q0.x;
+          const float psi1 = (bz * d11) + Q0.y;
+          sts2(ZZo + i * NX, (bz * tmp0) + (az * Z.x), (bz * tmp1) + (az * Z.y));
+          sts2(APZn + i * NX, az * psi0, az * psi1);
+        } else {
+          w0 = w0 + d2z0;
+          w1 = w1 + d2z1;
+        }
+        const float2 v = __ldg(reinterpret_cast<const float2*>(vel + i * NX));
+        const float v20 = v.x * v.x * dt2, v21 = v.y * v.y * dt2;
+        if (STORE) {
+          *reinterpret_cast<float2*>(st + i * NX) = make_float2(((2.0f * v.x) * dt2) * w0, ((2.0f * v.y) * dt2) * w1);
+        }
+        float n0 = ((v20 * w0) + (2.0f * u0)) - un[i][0];
+        float n1 = ((v21 * w1) + (2.0f * u1)) - un[i][1];
+        if (srcmask & (3u << (2 * i))) {
+          const int cell = gbase + i * NX;
+#pragma unroll
+          for (int k = 0; k < 4; ++k) {
+            const float wk_ = p.st.src_w[4 * shot + k];
+            if (cell == sc[k]) n0 = n0 + (((-v20) * wk_) * f);
+            if (cell + 1 == sc[k]) n1 = n1 + (((-v21) * wk_) * f);
+          }
+        }
+        un[i][0] = n0;
+        un[i][1] = n1;
+        sts2(Un + i * NX, n0, n1);
+        if constexpr (C > 1) {
+          if (rank > 0 && z < r0 + FD_PAD) st_peer_v2(U + (1 - par) * ustride + (z - pr_lo) * NX + x, rank - 1, n0, n1);
+          if (rank < C - 1 && z >= r1 - FD_PAD)
+            st_peer_v2(U + (1 - par) * ustride + (z - (r1 - FD_PAD)) * NX + x, rank + 1, n0, n1);
+        }
+      }
+    }
+    step_barrier<C>();
+  };
+
+  int t = p.t0;
+  for (; t + 1 < p.t1; t += 2) {
+    step(t, uA, uB);
+    step(t + 1, uB, uA);
+  }
+  if (t < p.t1) step(t, uA, uB);
+}
+
+// ------------------------------------------------------------------------------------------------
+// Adjoint (splatAdjoint.wgsl:58-131)
+// ------------------------------------------------------------------------------------------------
+template <int NX, int PMLP, int C, int S, int NSEG, int NI>
+__global__ void __launch_bounds__(NSEG * 32 * (1 + NI), 1) adj3_kernel(const __grid_constant__ AdjArgs p) {
+  using CL = Cols3<NX, PMLP>;
+  constexpr int SW = CL::SW;
+  constexpr int NT = NSEG * 32 * (1 + NI);
+  extern __shared__ __align__(16) float sm[];
+  const Grid& g = p.g;
+  const int nz = g.nz, swa = g.swa, region = g.region_adj, nrec = p.st.nrec, nt = g.nt;
+  const float rh = g.rh, dt2 = g.dt2;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int seg = warp / (1 + NI), wk = warp % (1 + NI);
+  const int rank = (C > 1) ? static_cast<int>(cluster_rank()) : 0;
+  const int unit = blockIdx.x / C;
+  const int shot = unit % p.st.shots;
+  const int model = unit / p.st.shots;
+  const size_t cells = static_cast<size_t>(NX) * nz;
+  const A3Layout L = a3_layout_rt(NX, PMLP, nz, swa, C);
+  const int r0 = split_row(nz, C, rank), r1 = split_row(nz, C, rank + 1);
+  const int zl0 = r0 - FD_PAD;
+  const int bot_off = (C == 1) ? swa : 0;
+  const int vstride = L.lr * NX, xstride = L.maxrows * 2 * SW, zstride = L.zs * NX;
+  float* sAX = sm + L.off_prof;
+  float* sBX = sAX + NX;
+  float* sDBX = sBX + NX;
+  float* sAZ = sDBX + NX;
+  float* sBZ = sAZ + nz;
+  float* sDBZ = sBZ + nz;
+
+  for (int i = tid; i < L.total; i += NT) sm[i] = 0.0f;
+  __syncthreads();
+  for (int i = tid; i < 3 * (NX + nz); i += NT) sAX[i] = g.prof[i];
+
+  const bool pml = (wk == 0);
+  const int x = CL::x_of(wk, lane);
+  const int zb = r0 + seg * S;
+  const int nrows = CL::active(wk, lane) ? max(0, min(S, r1 - zb)) : 0;
+  const bool xedge = !pml && (x < SW || x + 1 >= NX - SW);  // interior pair inside a T/U1 strip
+  const int vbase = (zb - zl0) * NX + x;
+  const int abase = (zb - r0) * 2 * SW + CL::strip(x);
+  const int zsh = (zb < nz / 2) ? 0 : (nz - swa - bot_off);
+  const int zbase = (zb - zsh) * NX + x;
+  const int gbase = zb * NX + x;
+  float* LPX = sm + L.off_lpx + abase;
+  float* LZX = sm + L.off_lzx + abase;
+  float* LPZ = sm + L.off_lpz + zbase;
+  float* LZZ = sm + L.off_lzz + zbase;
+
+  // per-column constants: (1 + b) of columns x-2 .. x+3; a, b, db of x, x+1
+  float opb[6], ax0 = 0.f, ax1 = 0.f, bx0 = 0.f, bx1 = 0.f, dbx0 = 0.f, dbx1 = 0.f;
+#pragma unroll
+  for (int k = 0; k < 6; ++k) opb[k] = 1.0f;
+  if (pml || xedge) {
+#pragma unroll
+    for (int k = 0; k < 6; ++k) opb[k] = 1.0f + g.prof[NX + x - 2 + k];
+    ax0 = g.prof[x];
+    ax1 = g.prof[x + 1];
+    bx0 = g.prof[NX + x];
+    bx1 = g.prof[NX + x + 1];
+    dbx0 = g.prof[2 * NX + x];
+    dbx1 = g.prof[2 * NX + x + 1];
+  }
+
+  float lA[S][2], lB[S][2], ga[S][2];
+  unsigned srcmask = 0, recmask = 0;
+  const int* sc = p.st.src_cell + 4 * shot;
+  const float* vel = p.vel + static_cast<size_t>(model) * cells + gbase;
+  const size_t asf = adjstate_floats(NX, nz, swa);
+  float* stt = p.state + static_cast<size_t>(unit) * asf;
+  float* sLc = stt;
+  float* sLp = stt + cells;
+  float* sPX = stt + 2 * cells;
+  float* sZX = sPX + static_cast<size_t>(nz) * 2 * swa;
+  float* sPZ = sZX + static_cast<size_t>(nz) * 2 * swa;
+  float* sZZ = sPZ + static_cast<size_t>(2) * swa * NX;
+  float* gacc = p.gacc + static_cast<size_t>(unit) * cells + gbase;
+  __syncthreads();
+#pragma unroll
+  for (int i = 0; i < S; ++i) {
+#pragma unroll
+    for (int j = 0; j < 2; ++j) lA[i][j] = lB[i][j] = ga[i][j] = 0.f;
+    if (i < nrows) {
+      const int z = zb + i;
+#pragma unroll
+      for (int j = 0; j < 2; ++j) {
+        const int cell = gbase + i * NX + j;
+        if (cell == sc[0] || cell == sc[1] || cell == sc[2] || cell == sc[3]) srcmask |= 1u << (2 * i + j);
+        if (p.st.csr[cell] < p.st.csr[cell + 1]) recmask |= 1u << (2 * i + j);
+        if (!p.first) {
+          lA[i][j] = sLc[cell];
+          lB[i][j] = sLp[cell];
+          ga[i][j] = gacc[i * NX + j];
+          const int xx = x + j;
+          if (xx < swa || xx >= NX - swa) {
+            const int xc = strip_col(xx, NX, swa);
+            LPX[i * 2 * SW + j] = sPX[z * 2 * swa + xc];
+            LZX[i * 2 * SW + j] = sZX[z * 2 * swa + xc];
+          }
+          if (z < swa || z >= nz - swa) {
+            const int zc = strip_col(z, nz, swa);
+            LPZ[i * NX + j] = sPZ[zc * NX + xx];
+            LZZ[i * NX + j] = sZZ[zc * NX + xx];
+          }
+        }
+      }
+    }
+  }
+  if constexpr (C > 1) cluster_barrier();
+  else __syncthreads();
+
+  const int pr_lo = (rank > 0) ? split_row(nz, C, rank - 1) - FD_PAD : 0;
+
+  // Derived terms of this thread's cells for lambda `lc` into buffer b.
+  auto derive = [&](int b, const float (&lc)[S][2]) {
+    float* VSb = sm + L.off_vs + b * vstride;
+    float* TXb = sm + L.off_tx + b * xstride + abase;
+    float* U1Xb = sm + L.off_u1x + b * xstride + abase;
+    float* TZb = sm + L.off_tz + b * zstride + zbase;
+    float* U1Zb = sm + L.off_u1z + b * zstride + zbase;
+#pragma unroll
+    for (int i = 0; i < S; ++i) {
+      if (i < nrows) {
+        const int z = zb + i;
+        const float2 v = __ldg(reinterpret_cast<const float2*>(vel + i * NX));
+        const float vs0 = (v.x * v.x * dt2) * lc[i][0];
+        const float vs1 = (v.y * v.y * dt2) * lc[i][1];
+        sts2(VSb + vbase + i * NX, vs0, vs1);
+        if constexpr (C > 1) {
+          if (rank > 0 && z < r0 + FD_PAD) st_peer_v2(VSb + (z - pr_lo) * NX + x, rank - 1, vs0, vs1);
+          if (rank < C - 1 && z >= r1 - FD_PAD) st_peer_v2(VSb + (z - (r1 - FD_PAD)) * NX + x, rank + 1, vs0, vs1);
+        }
+        if (pml) {
+          const float2 Z = lds2(LZX + i * 2 * SW);
+          const float2 P = lds2(LPX + i * 2 * SW);
+          const float T0 = (opb[2] * vs0) + (bx0 * Z.x);
+          const float T1 = (opb[3] * vs1) + (bx1 * Z.y);
+          sts2(TXb + i * 2 * SW, T0, T1);
+          sts2(U1Xb + i * 2 * SW, (dbx0 * T0) + (bx0 * P.x), (dbx1 * T1) + (bx1 * P.y));
+        } else if (xedge) {
+          // outside the adjoint region b = db = 0 and the adjoint psi, zeta are zero
+          const float T0 = (opb[2] * vs0) + (bx0 * 0.0f);
+          const float T1 = (opb[3] * vs1) + (bx1 * 0.0f);
+          sts2(TXb + i * 2 * SW, T0, T1);
+          sts2(U1Xb + i * 2 * SW, (dbx0 * T0) + (bx0 * 0.0f), (dbx1 * T1) + (bx1 * 0.0f));
+        }
+        if (z < swa || z >= nz - swa) {
+          const float bz = sBZ[z], dbz = sDBZ[z];
+          const float opbz = 1.0f + bz;
+          const float2 Z = lds2(LZZ + i * NX);
+          const float2 P = lds2(LPZ + i * NX);
+          const float T0 = (opbz * vs0) + (bz * Z.x);
+          const float T1 = (opbz * vs1) + (bz * Z.y);
+          sts2(TZb + i * NX, T0, T1);
+          sts2(U1Zb + i * NX, (dbz * T0) + (bz * P.x), (dbz * T1) + (bz * P.y));
+        }
+      }
+    }
+  };
+
+  derive(0, lA);
+  step_barrier<C>();
+
+  const int segn = p.t_hi - p.t_lo;
+  // One reverse step at time t: `lc` holds lambda at t, `lp` holds the previous one and receives
+  // the next.
+  auto step = [&](int t, float (&lc)[S][2], float (&lp)[S][2]) {
+    const int par = (p.t_hi - 1 - t) & 1;
+    const float* VSd = sm + L.off_vs + par * vstride + vbase;
+    const float* TXd = sm + L.off_tx + par * xstride + abase;
+    const float* U1Xd = sm + L.off_u1x + par * xstride + abase;
+    const float* TZd = sm + L.off_tz + par * zstride + zbase;
+    const float* U1Zd = sm + L.off_u1z + par * zstride + zbase;
+    const float f = __ldg(&g.wavelet[t]);
+    const float* st_t = p.stored + (static_cast<size_t>(unit) * segn + (t - p.t_lo)) * cells + gbase;
+    const float* res_t = p.residual + (static_cast<size_t>(unit) * nt + t) * nrec;
+    float2 stv[S];
+#pragma unroll
+    for (int i = 0; i < S; ++i)
+      stv[i] = (i < nrows) ? __ldcs(reinterpret_cast<const float2*>(st_t + i * NX)) : make_float2(0.f, 0.f);
+#pragma unroll
+    for (int i = 0; i < S; ++i) {
+      if (i < nrows) {
+        const int z = zb + i;
+        const float2 Vb = lds2(VSd + i * NX);  // own v^2 dt^2 lambda
+        float w0, w1;
+        if (pml) {
+          const float2 Ta = lds2(TXd + i * 2 * SW - 2), Tb = lds2(TXd + i * 2 * SW), Tc = lds2(TXd + i * 2 * SW + 2);
+          const float2 Ua = lds2(U1Xd + i * 2 * SW - 2), Ub = lds2(U1Xd + i * 2 * SW),
+                       Uc = lds2(U1Xd + i * 2 * SW + 2);
+          const float q0 = opb[0] * Ta.x, q1 = opb[1] * Ta.y, q2 = opb[2] * Tb.x, q3 = opb[3] * Tb.y,
+                      q4 = opb[4] * Tc.x, q5 = opb[5] * Tc.y;
+          // cell x: neighbours x-2..x+2 = (Ta.x, Ta.y, Tb.x, Tb.y, Tc.x)
+          const float du0 = ((F_D1A * (Ub.y - Ua.y)) + (A_D1B * (Uc.x - Ua.x))) * rh;
+          const float dd0 = ((((F_D2A * q2) + (F_D2B * (q3 + q1))) + (A_D2C * (q4 + q0))) * rh) * rh;
+          const float dt0 = ((F_D1A * (Tb.y - Ta.y)) + (A_D1B * (Tc.x - Ta.x))) * rh;
+          // cell x+1: neighbours x-1..x+3 = (Ta.y, Tb.x, Tb.y, Tc.x, Tc.y)
+          const float du1 = ((F_D1A * (Uc.x - Ub.x)) + (A_D1B * (Uc.y - Ua.y))) * rh;
+          const float dd1 = ((((F_D2A * q3) + (F_D2B * (q4 + q2))) + (A_D2C * (q5 + q1))) * rh) * rh;
+          const float dt1 = ((F_D1A * (Tc.x - Tb.x)) + (A_D1B * (Tc.y - Ta.y))) * rh;
+          w0 = (-du0) + dd0;
+          w1 = (-du1) + dd1;
+          const float2 P = lds2(LPX + i * 2 * SW);
+          const float2 Z = lds2(LZX + i * 2 * SW);
+          sts2(LPX + i * 2 * SW, ((-ax0) * dt0) + (ax0 * P.x), ((-ax1) * dt1) + (ax1 * P.y));
+          sts2(LZX + i * 2 * SW, (ax0 * Vb.x) + (ax0 * Z.x), (ax1 * Vb.y) + (ax1 * Z.y));
+        } else {
+          const float2 Va = lds2(VSd + i * NX - 2), Vc = lds2(VSd + i * NX + 2);
+          w0 = ((((F_D2A * Vb.x) + (F_D2B * (Vb.y + Va.y))) + (A_D2C * (Vc.x + Va.x))) * rh) * rh;
+          w1 = ((((F_D2A * Vb.y) + (F_D2B * (Vc.x + Vb.x))) + (A_D2C * (Vc.y + Va.y))) * rh) * rh;
+        }
+        if (z < region || z >= nz - region) {
+          const float2 Tm2 = lds2(TZd + (i - 2) * NX), Tm1 = lds2(TZd + (i - 1) * NX), T0 = lds2(TZd + i * NX),
+                       Tp1 = lds2(TZd + (i + 1) * NX), Tp2 = lds2(TZd + (i + 2) * NX);
+          const float2 Um2 = lds2(U1Zd + (i - 2) * NX), Um1 = lds2(U1Zd + (i - 1) * NX),
+                       Up1 = lds2(U1Zd + (i + 1) * NX), Up2 = lds2(U1Zd + (i + 2) * NX);
+          const float om2 = 1.0f + sBZ[z - 2], om1 = 1.0f + sBZ[z - 1], o0 = 1.0f + sBZ[z], op1 = 1.0f + sBZ[z + 1],
+                      op2 = 1.0f + sBZ[z + 2];
+          const float du0 = ((F_D1A * (Up1.x - Um1.x)) + (A_D1B * (Up2.x - Um2.x))) * rh;
+          const float du1 = ((F_D1A * (Up1.y - Um1.y)) + (A_D1B * (Up2.y - Um2.y))) * rh;
+          const float dd0 = ((((F_D2A * (o0 * T0.x)) + (F_D2B * ((op1 * Tp1.x) + (om1 * Tm1.x)))) +
+                              (A_D2C * ((op2 * Tp2.x) + (om2 * Tm2.x)))) * rh) * rh;
+          const float dd1 = ((((F_D2A * (o0 * T0.y)) + (F_D2B * ((op1 * Tp1.y) + (om1 * Tm1.y)))) +
+                              (A_D2C * ((op2 * Tp2.y) + (om2 * Tm2.y)))) * rh) * rh;
+          const float dt0 = ((F_D1A * (Tp1.x - Tm1.x)) + (A_D1B * (Tp2.x - Tm2.x))) * rh;
+          const float dt1 = ((F_D1A * (Tp1.y - Tm1.y)) + (A_D1B * (Tp2.y - Tm2.y))) * rh;
+          w0 = w0 + ((-du0) + dd0);
+          w1 = w1 + ((-du1) + dd1);
+          const float az = sAZ[z];
+          const float2 P = lds2(LPZ + i * NX);
+          const float2 Z = lds2(LZZ + i * NX);
+          sts2(LPZ + i * NX, ((-az) * dt0) + (az * P.x), ((-az) * dt1) + (az * P.y));
+          sts2(LZZ + i * NX, (az * Vb.x) + (az * Z.x), (az * Vb.y) + (az * Z.y));
+        } else {
+          const float2 Vm2 = lds2(VSd + (i - 2) * NX), Vm1 = lds2(VSd + (i - 1) * NX), Vp1 = lds2(VSd + (i + 1) * NX),
+                       Vp2 = lds2(VSd + (i + 2) * NX);
+          w0 = w0 + ((((F_D2A * Vb.x) + (F_D2B * (Vp1.x + Vm1.x))) + (A_D2C * (Vp2.x + Vm2.x))) * rh) * rh;
+          w1 = w1 + ((((F_D2A * Vb.y) + (F_D2B * (Vp1.y + Vm1.y))) + (A_D2C * (Vp2.y + Vm2.y))) * rh) * rh;
+        }
+        float n0 = (w0 + (2.0f * lc[i][0])) - lp[i][0];
+        float n1 = (w1 + (2.0f * lc[i][1])) - lp[i][1];
+        float g0 = 0.0f + ((lc[i][0] * stv[i].x) * 1.0f);
+        float g1 = 0.0f + ((lc[i][1] * stv[i].y) * 1.0f);
+        if (recmask & (3u << (2 * i))) {
+          const int cell = gbase + i * NX;
+          const int e1 = p.st.csr[cell + 1], e2 = p.st.csr[cell + 2];
+          for (int e = p.st.csr[cell]; e < e1; ++e) n0 = n0 + (p.st.ent_w[e] * res_t[p.st.ent_rec[e]]);
+          for (int e = e1; e < e2; ++e) n1 = n1 + (p.st.ent_w[e] * res_t[p.st.ent_rec[e]]);
+        }
+        if (srcmask & (3u << (2 * i))) {
+          const int cell = gbase + i * NX;
+          const float2 v = __ldg(reinterpret_cast<const float2*>(vel + i * NX));
+#pragma unroll
+          for (int k = 0; k < 4; ++k) {
+            const float wk_ = p.st.src_w[4 * shot + k];
+            if (cell == sc[k]) g0 = g0 + lc[i][0] * (((((-2.0f) * v.x) * dt2) * wk_) * f);
+            if (cell + 1 == sc[k]) g1 = g1 + lc[i][1] * (((((-2.0f) * v.y) * dt2) * wk_) * f);
+          }
+        }
+        ga[i][0] = ga[i][0] + g0;
+        ga[i][1] = ga[i][1] + g1;
+        lp[i][0] = n0;
+        lp[i][1] = n1;
+      }
+    }
+    if (t > p.t_lo) derive(1 - par, lp);
+    step_barrier<C>();
+  };
+
+  int t = p.t_hi - 1;
+  int flips = 0;
+  for (; t - 1 >= p.t_lo; t -= 2) {
+    step(t, lA, lB);
+    step(t - 1, lB, lA);
+  }
+  if (t >= p.t_lo) {
+    step(t, lA, lB);
+    flips = 1;
+  }
+  // after an odd number of steps lB holds the current lambda and lA the previous one
+#pragma unroll
+  for (int i = 0; i < S; ++i) {
+    if (i < nrows) {
+      const int z = zb + i;
+#pragma unroll
+      for (int j = 0; j < 2; ++j) {
+        const int cell = gbase + i * NX + j;
+        sLc[cell] = flips ? lB[i][j] : lA[i][j];
+        sLp[cell] = flips ? lA[i][j] : lB[i][j];
+        gacc[i * NX + j] = ga[i][j];
+        const int xx = x + j;
+        if (xx < swa || xx >= NX - swa) {
+          const int xc = strip_col(xx, NX, swa);
+          sPX[z * 2 * swa + xc] = LPX[i * 2 * SW + j];
+          sZX[z * 2 * swa + xc] = LZX[i * 2 * SW + j];
+        }
+        if (z < swa || z >= nz - swa) {
+          const int zc = strip_col(z, nz, swa);
+          sPZ[zc * NX + xx] = LPZ[i * NX + j];
+          sZZ[zc * NX + xx] = LZZ[i * NX + j];
+        }
+      }
+    }
+  }
+}
+
+template <int NX, int PMLP, int C, int S, int NSEG, int NI>
+cudaError_t fwd3_dispatch_impl(bool traces, bool store, const FwdArgs& a, size_t smem, cudaStream_t s) {
+  constexpr int NT = NSEG * 32 * (1 + NI);
+  if (traces && store)
+    return launch_cluster(fwd3_kernel<NX, PMLP, C, S, NSEG, NI, true, true>, C, NT, a.units, smem, s, a);
+  if (traces) return launch_cluster(fwd3_kernel<NX, PMLP, C, S, NSEG, NI, true, false>, C, NT, a.units, smem, s, a);
+  if (store) return launch_cluster(fwd3_kernel<NX, PMLP, C, S, NSEG, NI, false, true>, C, NT, a.units, smem, s, a);
+  return cudaErrorInvalidValue;
+}
+
+template <int NX, int PMLP, int C, int S, int NSEG, int NI>
+cudaError_t adj3_dispatch_impl(const AdjArgs& a, size_t smem, cudaStream_t s) {
+  constexpr int NT = NSEG * 32 * (1 + NI);
+  return launch_cluster(adj3_kernel<NX, PMLP, C, S, NSEG, NI>, C, NT, a.units, smem, s, a);
+}
+
+}  // namespace wg

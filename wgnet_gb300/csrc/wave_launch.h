@@ -26,8 +26,10 @@ template <int C, int NT, int CPT>
 cudaError_t fwd_dispatch(bool traces, bool store, const FwdArgs& a, size_t smem, cudaStream_t s);
 template <int C, int NT, int CPT>
 cudaError_t adj_dispatch(const AdjArgs& a, size_t smem, cudaStream_t s);
-template <int C, int S, int NSEG, int NI>
-cudaError_t fwd2_dispatch(bool traces, bool store, const FwdArgs& a, size_t smem, cudaStream_t s);
+template <int NX, int PMLP, int C, int S, int NSEG, int NI>
+cudaError_t fwd3_dispatch(bool traces, bool store, const FwdArgs& a, size_t smem, cudaStream_t s);
+template <int NX, int PMLP, int C, int S, int NSEG, int NI>
+cudaError_t adj3_dispatch(const AdjArgs& a, size_t smem, cudaStream_t s);
 
 // Forward over units = models * shots. traces: record receivers; store: write 2 v dt^2 w.
 cudaError_t launch_fwd(const Shape& s, bool traces, bool store, const FwdArgs& a, cudaStream_t stream);
