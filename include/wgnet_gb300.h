@@ -83,6 +83,12 @@ int wg_evaluate_adjoint_dev(wg_engine* eng, const float* d_vel_mps, const float*
 int wg_set_checkpoint_interval(wg_engine* eng, int k);
 int wg_get_checkpoint_interval(const wg_engine* eng);
 
+/* Named tuning options: "checkpoint_every" (as wg_set_checkpoint_interval), "adjoint_prefetch"
+ * (0/1: the column-pair adjoint fetches the next step's stored terms one step ahead). No
+ * reference counterpart. */
+int wg_set_option(wg_engine* eng, const char* key, int value);
+int wg_get_option(const wg_engine* eng, const char* key, int* value);
+
 /* Launch shape of the resident kernels (which = 0 forward, 1 adjoint): CTAs per (model, shot)
  * cluster, threads per CTA, cells-per-thread bound. wg_shape_candidates lists the compiled
  * shapes that fit this engine's grid. No reference counterpart (wgpu dispatches 16x16 tiles). */

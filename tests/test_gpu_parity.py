@@ -307,8 +307,10 @@ def test_every_adjoint_shape_bitexact_70x70(cuda_lib, k):
     rl, rg = o.evaluate_adjoint(sv, cur, src, wav, obs)
     shapes = eng.shape_candidates("adjoint")
     assert len(shapes) >= 3
-    for shape in shapes:
-        eng.set_launch_shape("adjoint", shape)
-        loss, grad = eng.evaluate_adjoint(cur, obs)
-        np.testing.assert_array_equal(grad, rg, err_msg=f"shape {shape}")
-        np.testing.assert_allclose(loss, rl, rtol=1e-12)
+    for pref in (0, 1):
+        eng.set_option("adjoint_prefetch", pref)
+        for shape in shapes:
+            eng.set_launch_shape("adjoint", shape)
+            loss, grad = eng.evaluate_adjoint(cur, obs)
+            np.testing.assert_array_equal(grad, rg, err_msg=f"shape {shape} prefetch {pref}")
+            np.testing.assert_allclose(loss, rl, rtol=1e-12)

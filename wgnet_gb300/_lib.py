@@ -50,6 +50,8 @@ SIGNATURES: dict[str, tuple] = {
     "wg_evaluate_adjoint_dev": (_I, [_P, _P, _P, _I, _P, _P, _P]),
     "wg_set_checkpoint_interval": (_I, [_P, _I]),
     "wg_get_checkpoint_interval": (_I, [_P]),
+    "wg_set_option": (_I, [_P, ctypes.c_char_p, _I]),
+    "wg_get_option": (_I, [_P, ctypes.c_char_p, ctypes.POINTER(_I)]),
     "wg_set_launch_shape": (_I, [_P, _I, _I, _I, _I]),
     "wg_get_launch_shape": (_I, [_P, _I, ctypes.POINTER(_I), ctypes.POINTER(_I), ctypes.POINTER(_I)]),
     "wg_shape_candidates": (_I, [_P, _I, _P, _I]),

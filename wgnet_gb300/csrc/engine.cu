@@ -143,6 +143,7 @@ struct wg_engine {
   DevBuf d_prof, d_wavelet, d_src_cell, d_src_w, d_rec_cell, d_rec_w, d_csr, d_ent_rec, d_ent_w, d_status;
   wg::Shape fshape{0, 0, 0}, ashape{0, 0, 0};
   int ck_every = 50;
+  int adj_prefetch = 0;
   // per-kernel timing: (kind, start, stop) events recorded on the launching stream
   bool prof_on = false;
   std::vector<int> prof_kind;
@@ -520,6 +521,7 @@ int gradient_dev_impl(wg_engine* e, const float* d_vis, const float* d_obs, int 
     a.state = e->w_adj.as<float>();
     a.gacc = e->w_gacc.as<float>();
     a.status = e->d_status.as<int>();
+    a.prefetch = e->adj_prefetch;
     if (store_all) {
       a.t_hi = e->nt;
       a.t_lo = 0;
@@ -587,6 +589,7 @@ EngineView engine_view(wg_engine* e, std::unique_lock<std::mutex>& lock) {
   v.fshape = e->fshape;
   v.ashape = e->ashape;
   v.d_status = e->d_status.as<int>();
+  v.adj_prefetch = e->adj_prefetch;
   return v;
 }
 
@@ -746,6 +749,33 @@ int wg_set_checkpoint_interval(wg_engine* e, int k) {
 }
 
 int wg_get_checkpoint_interval(const wg_engine* e) { return e ? e->ck_every : -1; }
+
+int wg_set_option(wg_engine* e, const char* key, int value) {
+  if (!e || !key) return fail(WG_ERR_ARG, "null argument");
+  std::lock_guard<std::mutex> lk(e->mu);
+  const std::string k(key);
+  if (k == "checkpoint_every") {
+    e->ck_every = value;
+  } else if (k == "adjoint_prefetch") {
+    e->adj_prefetch = value ? 1 : 0;
+  } else {
+    return fail(WG_ERR_ARG, "unknown option: " + k);
+  }
+  return WG_OK;
+}
+
+int wg_get_option(const wg_engine* e, const char* key, int* value) {
+  if (!e || !key || !value) return fail(WG_ERR_ARG, "null argument");
+  const std::string k(key);
+  if (k == "checkpoint_every") {
+    *value = e->ck_every;
+  } else if (k == "adjoint_prefetch") {
+    *value = e->adj_prefetch;
+  } else {
+    return fail(WG_ERR_ARG, "unknown option: " + k);
+  }
+  return WG_OK;
+}
 
 int wg_set_launch_shape(wg_engine* e, int which, int cluster, int threads, int cpt) {
   if (!e) return fail(WG_ERR_ARG, "null engine");

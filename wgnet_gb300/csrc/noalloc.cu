@@ -175,6 +175,7 @@ extern "C" int wg_evaluate_adjoint_noalloc(wg_engine* eng, const float* d_vel_mp
   a.state = adj;
   a.gacc = gacc;
   a.status = v.d_status;
+  a.prefetch = v.adj_prefetch;
   for (int j = J - 1; j >= 0; --j) {
     const int t0 = j * k, t1 = std::min(t0 + k, v.nt);
     wg::FwdArgs r{};

@@ -97,6 +97,7 @@ struct AdjArgs {
   int first;             // 1: start from zero state and zero gradient
   float* gacc;           // [units][nz][nx] gradient accumulator (per shot, padded grid)
   int* status;
+  int prefetch;          // generation-3 adjoint: fetch the next step's stored terms a step ahead
 };
 
 // Status codes shared with the C ABI (include/wgnet_gb300.h defines the same numbers).

@@ -30,6 +30,17 @@ __device__ __forceinline__ void st_peer(const float* local_ptr, unsigned peer, f
   asm volatile("st.shared::cluster.f32 [%0], %1;" ::"r"(ra), "f"(v) : "memory");
 }
 
+// Split cluster barrier. Threads that stored into a peer CTA's shared memory since the last barrier
+// fence first (cluster scope), so the relaxed arrive that follows publishes their stores to the
+// peers' acquiring wait; independent work can run between arrive and wait.
+__device__ __forceinline__ void fence_cluster() { asm volatile("fence.acq_rel.cluster;" ::: "memory"); }
+__device__ __forceinline__ void cluster_arrive_relaxed() {
+  asm volatile("barrier.cluster.arrive.relaxed.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void cluster_wait_acquire() {
+  asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+
 template <int C>
 __device__ __forceinline__ void step_barrier() {
   if constexpr (C == 1) {

@@ -10,7 +10,7 @@ cudaError_t fwd3_dispatch<114, 12, 2, 5, 11, 1>(bool traces, bool store, const F
 
 template <>
 cudaError_t adj3_dispatch<114, 12, 2, 5, 11, 1>(const AdjArgs& a, size_t smem, cudaStream_t s) {
-  return adj3_dispatch_impl<114, 12, 2, 5, 11, 1>(a, smem, s);
+  return adj3_dispatch_impl_pref<114, 12, 2, 5, 11, 1>(a, smem, s);
 }
 
 }  // namespace wg

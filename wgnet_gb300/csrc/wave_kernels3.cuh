@@ -52,7 +52,7 @@ __device__ __forceinline__ void st_peer_v2(const float* local_ptr, unsigned peer
 // ------------------------------------------------------------------------------------------------
 // Forward (splatForward.wgsl:48-121)
 // ------------------------------------------------------------------------------------------------
-template <int NX, int PMLP, int C, int S, int NSEG, int NI, bool TRACES, bool STORE>
+template <int NX, int PMLP, int C, int S, int NSEG, int NI, bool FULL, bool TRACES, bool STORE>
 __global__ void __launch_bounds__(NSEG * 32 * (1 + NI), 1) fwd3_kernel(const __grid_constant__ FwdArgs p) {
   using CL = Cols3<NX, PMLP>;
   constexpr int SW = CL::SW;
@@ -104,7 +104,9 @@ __global__ void __launch_bounds__(NSEG * 32 * (1 + NI), 1) fwd3_kernel(const __g
   const bool pml = (wk == 0);
   const int x = CL::x_of(wk, lane);
   const int zb = r0 + seg * S;
-  const int nrows = CL::active(wk, lane) ? max(0, min(S, r1 - zb)) : 0;
+  // FULL: every segment of every CTA has exactly S rows (checked on the host)
+  const int nrows = CL::active(wk, lane) ? (FULL ? S : max(0, min(S, r1 - zb))) : 0;
+  const bool pusher = (C > 1) && nrows > 0 && ((rank > 0 && zb < r0 + FD_PAD) || (rank < C - 1 && zb + nrows > r1 - FD_PAD));
   const int ubase = (zb - zl0) * NX + x;                 // row 0 of the segment in U
   const int abase = (zb - r0) * 2 * SW + CL::strip(x);   // row 0 in APX / ZX (PML warp)
   const int zsh = (zb < nz / 2) ? 0 : (nz - sw - bot_off);
@@ -126,10 +128,15 @@ __global__ void __launch_bounds__(NSEG * 32 * (1 + NI), 1) fwd3_kernel(const __g
   unsigned srcmask = 0;
   const int* sc = p.st.src_cell + 4 * shot;
   const float* vel = p.vel + static_cast<size_t>(model) * cells + gbase;
+  float* V2o = sm + L.off_v2 + (zb - r0) * NX + x;  // owner-only coefficient rows
+  float* C2o = sm + L.off_c2 + (zb - r0) * NX + x;
 #pragma unroll
   for (int i = 0; i < S; ++i) {
     uA[i][0] = uA[i][1] = uB[i][0] = uB[i][1] = 0.f;
     if (i < nrows) {
+      const float2 v = __ldg(reinterpret_cast<const float2*>(vel + i * NX));
+      sts2(V2o + i * NX, v.x * v.x * dt2, v.y * v.y * dt2);
+      if (STORE) sts2(C2o + i * NX, (2.0f * v.x) * dt2, (2.0f * v.y) * dt2);
       const int cell = gbase + i * NX;
       if (cell == sc[0] || cell == sc[1] || cell == sc[2] || cell == sc[3]) srcmask |= 1u << (2 * i);
       if (cell + 1 == sc[0] || cell + 1 == sc[1] || cell + 1 == sc[2] || cell + 1 == sc[3])
@@ -234,6 +241,7 @@ __global__ void __launch_bounds__(NSEG * 32 * (1 + NI), 1) fwd3_kernel(const __g
 
     const float f = __ldg(&g.wavelet[t]);
     float* st = STORE ? p.stored + (static_cast<size_t>(unit) * (p.t1 - p.t0) + (t - p.t0)) * cells + gbase : nullptr;
+    float2 stv[STORE ? S : 1];
 #pragma unroll
     for (int i = 0; i < S; ++i) {
       if (i < nrows) {
@@ -257,7 +265,7 @@ __global__ void __launch_bounds__(NSEG * 32 * (1 + NI), 1) fwd3_kernel(const __g
           zm1[0] = q.x;
           zm1[1] = q.y;
         }
-        if (i + 1 < S && i + 1 < nrows) {
+        if (i + 1 < S && (FULL || i + 1 < nrows)) {
           zp1[0] = uc[i + 1 < S ? i + 1 : i][0];
           zp1[1] = uc[i + 1 < S ? i + 1 : i][1];
         } else {
@@ -265,7 +273,7 @@ __global__ void __launch_bounds__(NSEG * 32 * (1 + NI), 1) fwd3_kernel(const __g
           zp1[0] = q.x;
           zp1[1] = q.y;
         }
-        if (i + 2 < S && i + 2 < nrows) {
+        if (i + 2 < S && (FULL || i + 2 < nrows)) {
           zp2[0] = uc[i + 2 < S ? i + 2 : i][0];
           zp2[1] = uc[i + 2 < S ? i + 2 : i][1];
         } else {
@@ -325,10 +333,11 @@ __global__ void __launch_bounds__(NSEG * 32 * (1 + NI), 1) fwd3_kernel(const __g
           w0 = w0 + d2z0;
           w1 = w1 + d2z1;
         }
-        const float2 v = __ldg(reinterpret_cast<const float2*>(vel + i * NX));
-        const float v20 = v.x * v.x * dt2, v21 = v.y * v.y * dt2;
+        const float2 vv = lds2(V2o + i * NX);
+        const float v20 = vv.x, v21 = vv.y;
         if (STORE) {
-          *reinterpret_cast<float2*>(st + i * NX) = make_float2(((2.0f * v.x) * dt2) * w0, ((2.0f * v.y) * dt2) * w1);
+          const float2 cc = lds2(C2o + i * NX);
+          stv[i] = make_float2(cc.x * w0, cc.y * w1);
         }
         float n0 = ((v20 * w0) + (2.0f * u0)) - un[i][0];
         float n1 = ((v21 * w1) + (2.0f * u1)) - un[i][1];
@@ -351,7 +360,18 @@ __global__ void __launch_bounds__(NSEG * 32 * (1 + NI), 1) fwd3_kernel(const __g
         }
       }
     }
-    step_barrier<C>();
+    if constexpr (C > 1) {
+      if (pusher) fence_cluster();
+      __syncthreads();
+      cluster_arrive_relaxed();
+    }
+    if (STORE) {  // the gradient terms go to global memory while the peers catch up
+#pragma unroll
+      for (int i = 0; i < S; ++i)
+        if (i < nrows) *reinterpret_cast<float2*>(st + i * NX) = stv[i];
+    }
+    if constexpr (C > 1) cluster_wait_acquire();
+    else __syncthreads();
   };
 
   int t = p.t0;
@@ -365,7 +385,9 @@ __global__ void __launch_bounds__(NSEG * 32 * (1 + NI), 1) fwd3_kernel(const __g
 // ------------------------------------------------------------------------------------------------
 // Adjoint (splatAdjoint.wgsl:58-131)
 // ------------------------------------------------------------------------------------------------
-template <int NX, int PMLP, int C, int S, int NSEG, int NI>
+// PREF: fetch the next step's stored gradient terms between the barrier's arrive and wait (2 S more
+// registers per thread) instead of loading each row's terms when the row is processed.
+template <int NX, int PMLP, int C, int S, int NSEG, int NI, bool FULL, bool PREF>
 __global__ void __launch_bounds__(NSEG * 32 * (1 + NI), 1) adj3_kernel(const __grid_constant__ AdjArgs p) {
   using CL = Cols3<NX, PMLP>;
   constexpr int SW = CL::SW;
@@ -400,7 +422,8 @@ __global__ void __launch_bounds__(NSEG * 32 * (1 + NI), 1) adj3_kernel(const __g
   const bool pml = (wk == 0);
   const int x = CL::x_of(wk, lane);
   const int zb = r0 + seg * S;
-  const int nrows = CL::active(wk, lane) ? max(0, min(S, r1 - zb)) : 0;
+  const int nrows = CL::active(wk, lane) ? (FULL ? S : max(0, min(S, r1 - zb))) : 0;
+  const bool pusher = (C > 1) && nrows > 0 && ((rank > 0 && zb < r0 + FD_PAD) || (rank < C - 1 && zb + nrows > r1 - FD_PAD));
   const bool xedge = !pml && (x < SW || x + 1 >= NX - SW);  // interior pair inside a T/U1 strip
   const int vbase = (zb - zl0) * NX + x;
   const int abase = (zb - r0) * 2 * SW + CL::strip(x);
@@ -412,20 +435,9 @@ __global__ void __launch_bounds__(NSEG * 32 * (1 + NI), 1) adj3_kernel(const __g
   float* LPZ = sm + L.off_lpz + zbase;
   float* LZZ = sm + L.off_lzz + zbase;
 
-  // per-column constants: (1 + b) of columns x-2 .. x+3; a, b, db of x, x+1
-  float opb[6], ax0 = 0.f, ax1 = 0.f, bx0 = 0.f, bx1 = 0.f, dbx0 = 0.f, dbx1 = 0.f;
-#pragma unroll
-  for (int k = 0; k < 6; ++k) opb[k] = 1.0f;
-  if (pml || xedge) {
-#pragma unroll
-    for (int k = 0; k < 6; ++k) opb[k] = 1.0f + g.prof[NX + x - 2 + k];
-    ax0 = g.prof[x];
-    ax1 = g.prof[x + 1];
-    bx0 = g.prof[NX + x];
-    bx1 = g.prof[NX + x + 1];
-    dbx0 = g.prof[2 * NX + x];
-    dbx1 = g.prof[2 * NX + x + 1];
-  }
+  // per-column constants live in shared memory: (1 + b) in sOPB, a, b, db in the profiles
+  float* sOPB = sm + L.off_opb;
+  for (int i = tid; i < NX; i += NT) sOPB[i] = 1.0f + g.prof[NX + i];
 
   float lA[S][2], lB[S][2], ga[S][2];
   unsigned srcmask = 0, recmask = 0;
@@ -495,19 +507,15 @@ __global__ void __launch_bounds__(NSEG * 32 * (1 + NI), 1) adj3_kernel(const __g
           if (rank > 0 && z < r0 + FD_PAD) st_peer_v2(VSb + (z - pr_lo) * NX + x, rank - 1, vs0, vs1);
           if (rank < C - 1 && z >= r1 - FD_PAD) st_peer_v2(VSb + (z - (r1 - FD_PAD)) * NX + x, rank + 1, vs0, vs1);
         }
-        if (pml) {
-          const float2 Z = lds2(LZX + i * 2 * SW);
-          const float2 P = lds2(LPX + i * 2 * SW);
-          const float T0 = (opb[2] * vs0) + (bx0 * Z.x);
-          const float T1 = (opb[3] * vs1) + (bx1 * Z.y);
+        if (pml || xedge) {
+          // outside the adjoint region (xedge) b = db = 0 and the adjoint psi, zeta are zero
+          const float2 o = lds2(sOPB + x), b = lds2(sBX + x), db = lds2(sDBX + x);
+          const float2 Z = pml ? lds2(LZX + i * 2 * SW) : make_float2(0.f, 0.f);
+          const float2 P = pml ? lds2(LPX + i * 2 * SW) : make_float2(0.f, 0.f);
+          const float T0 = (o.x * vs0) + (b.x * Z.x);
+          const float T1 = (o.y * vs1) + (b.y * Z.y);
           sts2(TXb + i * 2 * SW, T0, T1);
-          sts2(U1Xb + i * 2 * SW, (dbx0 * T0) + (bx0 * P.x), (dbx1 * T1) + (bx1 * P.y));
-        } else if (xedge) {
-          // outside the adjoint region b = db = 0 and the adjoint psi, zeta are zero
-          const float T0 = (opb[2] * vs0) + (bx0 * 0.0f);
-          const float T1 = (opb[3] * vs1) + (bx1 * 0.0f);
-          sts2(TXb + i * 2 * SW, T0, T1);
-          sts2(U1Xb + i * 2 * SW, (dbx0 * T0) + (bx0 * 0.0f), (dbx1 * T1) + (bx1 * 0.0f));
+          sts2(U1Xb + i * 2 * SW, (db.x * T0) + (b.x * P.x), (db.y * T1) + (b.y * P.y));
         }
         if (z < swa || z >= nz - swa) {
           const float bz = sBZ[z], dbz = sDBZ[z];
@@ -527,6 +535,14 @@ __global__ void __launch_bounds__(NSEG * 32 * (1 + NI), 1) adj3_kernel(const __g
   step_barrier<C>();
 
   const int segn = p.t_hi - p.t_lo;
+  // stored gradient terms of the next step to process, loaded one step ahead (PREF)
+  float2 stv[PREF ? S : 1];
+  if (PREF) {
+    const float* st0 = p.stored + (static_cast<size_t>(unit) * segn + (p.t_hi - 1 - p.t_lo)) * cells + gbase;
+#pragma unroll
+    for (int i = 0; i < S; ++i)
+      stv[i] = (i < nrows) ? __ldcs(reinterpret_cast<const float2*>(st0 + i * NX)) : make_float2(0.f, 0.f);
+  }
   // One reverse step at time t: `lc` holds lambda at t, `lp` holds the previous one and receives
   // the next.
   auto step = [&](int t, float (&lc)[S][2], float (&lp)[S][2]) {
@@ -537,12 +553,8 @@ __global__ void __launch_bounds__(NSEG * 32 * (1 + NI), 1) adj3_kernel(const __g
     const float* TZd = sm + L.off_tz + par * zstride + zbase;
     const float* U1Zd = sm + L.off_u1z + par * zstride + zbase;
     const float f = __ldg(&g.wavelet[t]);
-    const float* st_t = p.stored + (static_cast<size_t>(unit) * segn + (t - p.t_lo)) * cells + gbase;
     const float* res_t = p.residual + (static_cast<size_t>(unit) * nt + t) * nrec;
-    float2 stv[S];
-#pragma unroll
-    for (int i = 0; i < S; ++i)
-      stv[i] = (i < nrows) ? __ldcs(reinterpret_cast<const float2*>(st_t + i * NX)) : make_float2(0.f, 0.f);
+    const float* st_t = p.stored + (static_cast<size_t>(unit) * segn + (t - p.t_lo)) * cells + gbase;
 #pragma unroll
     for (int i = 0; i < S; ++i) {
       if (i < nrows) {
@@ -553,8 +565,9 @@ __global__ void __launch_bounds__(NSEG * 32 * (1 + NI), 1) adj3_kernel(const __g
           const float2 Ta = lds2(TXd + i * 2 * SW - 2), Tb = lds2(TXd + i * 2 * SW), Tc = lds2(TXd + i * 2 * SW + 2);
           const float2 Ua = lds2(U1Xd + i * 2 * SW - 2), Ub = lds2(U1Xd + i * 2 * SW),
                        Uc = lds2(U1Xd + i * 2 * SW + 2);
-          const float q0 = opb[0] * Ta.x, q1 = opb[1] * Ta.y, q2 = opb[2] * Tb.x, q3 = opb[3] * Tb.y,
-                      q4 = opb[4] * Tc.x, q5 = opb[5] * Tc.y;
+          const float2 Oa = lds2(sOPB + x - 2), Ob = lds2(sOPB + x), Oc = lds2(sOPB + x + 2);
+          const float q0 = Oa.x * Ta.x, q1 = Oa.y * Ta.y, q2 = Ob.x * Tb.x, q3 = Ob.y * Tb.y, q4 = Oc.x * Tc.x,
+                      q5 = Oc.y * Tc.y;
           // cell x: neighbours x-2..x+2 = (Ta.x, Ta.y, Tb.x, Tb.y, Tc.x)
           const float du0 = ((F_D1A * (Ub.y - Ua.y)) + (A_D1B * (Uc.x - Ua.x))) * rh;
           const float dd0 = ((((F_D2A * q2) + (F_D2B * (q3 + q1))) + (A_D2C * (q4 + q0))) * rh) * rh;
@@ -567,8 +580,9 @@ __global__ void __launch_bounds__(NSEG * 32 * (1 + NI), 1) adj3_kernel(const __g
           w1 = (-du1) + dd1;
           const float2 P = lds2(LPX + i * 2 * SW);
           const float2 Z = lds2(LZX + i * 2 * SW);
-          sts2(LPX + i * 2 * SW, ((-ax0) * dt0) + (ax0 * P.x), ((-ax1) * dt1) + (ax1 * P.y));
-          sts2(LZX + i * 2 * SW, (ax0 * Vb.x) + (ax0 * Z.x), (ax1 * Vb.y) + (ax1 * Z.y));
+          const float2 a = lds2(sAX + x);
+          sts2(LPX + i * 2 * SW, ((-a.x) * dt0) + (a.x * P.x), ((-a.y) * dt1) + (a.y * P.y));
+          sts2(LZX + i * 2 * SW, (a.x * Vb.x) + (a.x * Z.x), (a.y * Vb.y) + (a.y * Z.y));
         } else {
           const float2 Va = lds2(VSd + i * NX - 2), Vc = lds2(VSd + i * NX + 2);
           w0 = ((((F_D2A * Vb.x) + (F_D2B * (Vb.y + Va.y))) + (A_D2C * (Vc.x + Va.x))) * rh) * rh;
@@ -604,8 +618,9 @@ __global__ void __launch_bounds__(NSEG * 32 * (1 + NI), 1) adj3_kernel(const __g
         }
         float n0 = (w0 + (2.0f * lc[i][0])) - lp[i][0];
         float n1 = (w1 + (2.0f * lc[i][1])) - lp[i][1];
-        float g0 = 0.0f + ((lc[i][0] * stv[i].x) * 1.0f);
-        float g1 = 0.0f + ((lc[i][1] * stv[i].y) * 1.0f);
+        const float2 sv = PREF ? stv[PREF ? i : 0] : __ldcs(reinterpret_cast<const float2*>(st_t + i * NX));
+        float g0 = 0.0f + ((lc[i][0] * sv.x) * 1.0f);
+        float g1 = 0.0f + ((lc[i][1] * sv.y) * 1.0f);
         if (recmask & (3u << (2 * i))) {
           const int cell = gbase + i * NX;
           const int e1 = p.st.csr[cell + 1], e2 = p.st.csr[cell + 2];
@@ -629,7 +644,19 @@ __global__ void __launch_bounds__(NSEG * 32 * (1 + NI), 1) adj3_kernel(const __g
       }
     }
     if (t > p.t_lo) derive(1 - par, lp);
-    step_barrier<C>();
+    if constexpr (C > 1) {
+      if (pusher) fence_cluster();
+      __syncthreads();
+      cluster_arrive_relaxed();
+    }
+    if (PREF && t > p.t_lo) {  // next step's stored terms, fetched while the peers catch up
+      const float* stn = p.stored + (static_cast<size_t>(unit) * segn + (t - 1 - p.t_lo)) * cells + gbase;
+#pragma unroll
+      for (int i = 0; i < S; ++i)
+        if (i < nrows) stv[PREF ? i : 0] = __ldcs(reinterpret_cast<const float2*>(stn + i * NX));
+    }
+    if constexpr (C > 1) cluster_wait_acquire();
+    else __syncthreads();
   };
 
   int t = p.t_hi - 1;
@@ -669,20 +696,48 @@ __global__ void __launch_bounds__(NSEG * 32 * (1 + NI), 1) adj3_kernel(const __g
   }
 }
 
-template <int NX, int PMLP, int C, int S, int NSEG, int NI>
-cudaError_t fwd3_dispatch_impl(bool traces, bool store, const FwdArgs& a, size_t smem, cudaStream_t s) {
-  constexpr int NT = NSEG * 32 * (1 + NI);
-  if (traces && store)
-    return launch_cluster(fwd3_kernel<NX, PMLP, C, S, NSEG, NI, true, true>, C, NT, a.units, smem, s, a);
-  if (traces) return launch_cluster(fwd3_kernel<NX, PMLP, C, S, NSEG, NI, true, false>, C, NT, a.units, smem, s, a);
-  if (store) return launch_cluster(fwd3_kernel<NX, PMLP, C, S, NSEG, NI, false, true>, C, NT, a.units, smem, s, a);
-  return cudaErrorInvalidValue;
+// Every segment of every CTA has exactly S rows when the CTAs' rows split evenly into NSEG segments.
+template <int C, int S, int NSEG>
+inline bool g3_full(int nz) {
+  for (int r = 0; r < C; ++r)
+    if (split_row(nz, C, r + 1) - split_row(nz, C, r) != S * NSEG) return false;
+  return true;
 }
 
 template <int NX, int PMLP, int C, int S, int NSEG, int NI>
+cudaError_t fwd3_dispatch_impl(bool traces, bool store, const FwdArgs& a, size_t smem, cudaStream_t s) {
+  constexpr int NT = NSEG * 32 * (1 + NI);
+  if (g3_full<C, S, NSEG>(a.g.nz)) {
+    if (traces && store)
+      return launch_cluster(fwd3_kernel<NX, PMLP, C, S, NSEG, NI, true, true, true>, C, NT, a.units, smem, s, a);
+    if (traces)
+      return launch_cluster(fwd3_kernel<NX, PMLP, C, S, NSEG, NI, true, true, false>, C, NT, a.units, smem, s, a);
+    if (store)
+      return launch_cluster(fwd3_kernel<NX, PMLP, C, S, NSEG, NI, true, false, true>, C, NT, a.units, smem, s, a);
+    return cudaErrorInvalidValue;
+  }
+  if (traces && store)
+    return launch_cluster(fwd3_kernel<NX, PMLP, C, S, NSEG, NI, false, true, true>, C, NT, a.units, smem, s, a);
+  if (traces)
+    return launch_cluster(fwd3_kernel<NX, PMLP, C, S, NSEG, NI, false, true, false>, C, NT, a.units, smem, s, a);
+  if (store)
+    return launch_cluster(fwd3_kernel<NX, PMLP, C, S, NSEG, NI, false, false, true>, C, NT, a.units, smem, s, a);
+  return cudaErrorInvalidValue;
+}
+
+template <int NX, int PMLP, int C, int S, int NSEG, int NI, bool PREF>
 cudaError_t adj3_dispatch_impl(const AdjArgs& a, size_t smem, cudaStream_t s) {
   constexpr int NT = NSEG * 32 * (1 + NI);
-  return launch_cluster(adj3_kernel<NX, PMLP, C, S, NSEG, NI>, C, NT, a.units, smem, s, a);
+  if (g3_full<C, S, NSEG>(a.g.nz))
+    return launch_cluster(adj3_kernel<NX, PMLP, C, S, NSEG, NI, true, PREF>, C, NT, a.units, smem, s, a);
+  return launch_cluster(adj3_kernel<NX, PMLP, C, S, NSEG, NI, false, PREF>, C, NT, a.units, smem, s, a);
+}
+
+// Adjoint launch: the prefetching variant when `pref` is set in the shape.
+template <int NX, int PMLP, int C, int S, int NSEG, int NI>
+cudaError_t adj3_dispatch_impl_pref(const AdjArgs& a, size_t smem, cudaStream_t s) {
+  if (a.prefetch) return adj3_dispatch_impl<NX, PMLP, C, S, NSEG, NI, true>(a, smem, s);
+  return adj3_dispatch_impl<NX, PMLP, C, S, NSEG, NI, false>(a, smem, s);
 }
 
 }  // namespace wg

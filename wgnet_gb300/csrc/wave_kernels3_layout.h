@@ -10,7 +10,7 @@ __host__ __device__ inline int g3_sw(int pmlp) { return 2 * pmlp + 4; }  // pack
 
 struct F3Layout {
   int maxrows, lr, zs;
-  int off_u, off_apx, off_zx, off_apz, off_zz, off_prof, off_rec, total;
+  int off_u, off_apx, off_zx, off_apz, off_zz, off_v2, off_c2, off_prof, off_rec, total;
 };
 
 __host__ __device__ inline F3Layout f3_layout_rt(int NX, int pmlp, int nz, int sw, int C, int nrec) {
@@ -24,7 +24,9 @@ __host__ __device__ inline F3Layout f3_layout_rt(int NX, int pmlp, int nz, int s
   L.off_zx = L.off_apx + 2 * L.maxrows * 2 * SW;  // ZX[maxrows][2 SW]      zeta_x (owner only)
   L.off_apz = L.off_zx + L.maxrows * 2 * SW;      // APZ[2][zs][NX]          a * psi_z
   L.off_zz = L.off_apz + 2 * L.zs * NX;           // ZZ[zs][NX]              zeta_z (owner only)
-  L.off_prof = L.off_zz + L.zs * NX;
+  L.off_v2 = L.off_zz + L.zs * NX;                // V2[maxrows][NX]         v^2 dt^2 (owner only)
+  L.off_c2 = L.off_v2 + L.maxrows * NX;           // C2[maxrows][NX]         2 v dt^2 (owner only)
+  L.off_prof = L.off_c2 + L.maxrows * NX;
   L.off_rec = L.off_prof + 3 * (NX + nz);
   L.total = (L.off_rec + 9 * nrec + 3) & ~3;
   return L;
@@ -32,7 +34,7 @@ __host__ __device__ inline F3Layout f3_layout_rt(int NX, int pmlp, int nz, int s
 
 struct A3Layout {
   int maxrows, lr, zs;
-  int off_vs, off_tx, off_u1x, off_tz, off_u1z, off_lpx, off_lzx, off_lpz, off_lzz, off_prof, total;
+  int off_vs, off_tx, off_u1x, off_tz, off_u1z, off_lpx, off_lzx, off_lpz, off_lzz, off_prof, off_opb, total;
 };
 
 __host__ __device__ inline A3Layout a3_layout_rt(int NX, int pmlp, int nz, int swa, int C) {
@@ -51,8 +53,9 @@ __host__ __device__ inline A3Layout a3_layout_rt(int NX, int pmlp, int nz, int s
   L.off_lzx = L.off_lpx + sx;             // LZX[maxrows][2 SW]  adjoint zeta_x
   L.off_lpz = L.off_lzx + sx;             // LPZ[zs][NX]
   L.off_lzz = L.off_lpz + sz;             // LZZ[zs][NX]
-  L.off_prof = L.off_lzz + sz;
-  L.total = (L.off_prof + 3 * (NX + nz) + 3) & ~3;
+  L.off_prof = L.off_lzz + sz;            // ax bx dbx az bz dbz
+  L.off_opb = L.off_prof + 3 * (NX + nz); // 1 + bx, per column
+  L.total = (L.off_opb + NX + 3) & ~3;
   return L;
 }
 

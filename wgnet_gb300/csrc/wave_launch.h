@@ -73,6 +73,7 @@ struct EngineView {
   float vmin, vmax;
   Shape fshape, ashape;
   int* d_status;
+  int adj_prefetch;
 };
 
 // out[i] = in[i] * alpha (unit conversion), n elements.

@@ -88,6 +88,14 @@ class WaveEngine:
     def checkpoint_every(self, k: int) -> None:
         check(self._lib.wg_set_checkpoint_interval(self._h, int(k)))
 
+    def set_option(self, key: str, value: int) -> None:
+        check(self._lib.wg_set_option(self._h, key.encode(), int(value)))
+
+    def get_option(self, key: str) -> int:
+        v = ctypes.c_int()
+        check(self._lib.wg_get_option(self._h, key.encode(), ctypes.byref(v)))
+        return v.value
+
     def launch_shape(self, which: str = "forward") -> tuple[int, int, int]:
         w = 0 if which.startswith("f") else 1
         c, t, k = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
