@@ -143,7 +143,7 @@ struct wg_engine {
   DevBuf d_prof, d_wavelet, d_src_cell, d_src_w, d_rec_cell, d_rec_w, d_csr, d_ent_rec, d_ent_w, d_status;
   wg::Shape fshape{0, 0, 0}, ashape{0, 0, 0};
   int ck_every = 50;
-  int adj_prefetch = 0;
+  int adj_prefetch = 1;
   // per-kernel timing: (kind, start, stop) events recorded on the launching stream
   bool prof_on = false;
   std::vector<int> prof_kind;
@@ -280,10 +280,10 @@ bool find_shape(int which, int cluster, int threads, int cpt, wg::Shape* out) {
 bool pick_shapes(wg_engine* e) {
   // Preference order; the first compiled shape that fits the grid is the default (the autotuner
   // can choose another among wg_shape_candidates).
-  static const int fpref[][3] = {{2, 896, 8}, {2, 704, 10}, {4, 896, 4}, {4, 448, 8}, {2, 1024, 6},
-                                 {1, 1024, 12}, {2, 512, 12}, {2, 1024, 10}, {4, 1024, 8}, {2, 1024, 16},
+  static const int fpref[][3] = {{2, 704, 10}, {2, 896, 8}, {4, 896, 4}, {4, 448, 8}, {1, 1024, 12},
+                                 {2, 1024, 6}, {2, 512, 12}, {2, 1024, 10}, {4, 1024, 8}, {2, 1024, 16},
                                  {4, 512, 16}};
-  static const int apref[][3] = {{4, 448, 8}, {4, 896, 4}, {2, 704, 10}, {2, 896, 8}, {2, 1024, 6},
+  static const int apref[][3] = {{2, 704, 10}, {2, 896, 8}, {2, 1024, 6}, {4, 896, 4}, {4, 448, 8},
                                  {2, 512, 12}, {4, 1024, 4}, {4, 1024, 8}, {4, 512, 16}};
   e->fshape = wg::Shape{0, 0, 0};
   e->ashape = wg::Shape{0, 0, 0};
