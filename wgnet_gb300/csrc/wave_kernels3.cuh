@@ -407,7 +407,7 @@ __global__ void __launch_bounds__(NSEG * 32 * (1 + NI), 1) adj3_kernel(const __g
   const int r0 = split_row(nz, C, rank), r1 = split_row(nz, C, rank + 1);
   const int zl0 = r0 - FD_PAD;
   const int bot_off = (C == 1) ? swa : 0;
-  const int vstride = L.lr * NX, xstride = L.maxrows * 2 * SW, zstride = L.zs * NX;
+  const int vstride = L.lr * NX;
   float* sAX = sm + L.off_prof;
   float* sBX = sAX + NX;
   float* sDBX = sBX + NX;
@@ -434,12 +434,18 @@ __global__ void __launch_bounds__(NSEG * 32 * (1 + NI), 1) adj3_kernel(const __g
   float* LZX = sm + L.off_lzx + abase;
   float* LPZ = sm + L.off_lpz + zbase;
   float* LZZ = sm + L.off_lzz + zbase;
+  float* TXs = sm + L.off_tx + abase;
+  float* U1Xs = sm + L.off_u1x + abase;
+  float* TZs = sm + L.off_tz + zbase;
+  float* U1Zs = sm + L.off_u1z + zbase;
+  float* V2o = sm + L.off_v2 + (zb - r0) * NX + x;
+  float* GAo = sm + L.off_ga + (zb - r0) * NX + x;
 
   // per-column constants live in shared memory: (1 + b) in sOPB, a, b, db in the profiles
   float* sOPB = sm + L.off_opb;
   for (int i = tid; i < NX; i += NT) sOPB[i] = 1.0f + g.prof[NX + i];
 
-  float lA[S][2], lB[S][2], ga[S][2];
+  float lA[S][2], lB[S][2];
   unsigned srcmask = 0, recmask = 0;
   const int* sc = p.st.src_cell + 4 * shot;
   const float* vel = p.vel + static_cast<size_t>(model) * cells + gbase;
@@ -456,9 +462,14 @@ __global__ void __launch_bounds__(NSEG * 32 * (1 + NI), 1) adj3_kernel(const __g
 #pragma unroll
   for (int i = 0; i < S; ++i) {
 #pragma unroll
-    for (int j = 0; j < 2; ++j) lA[i][j] = lB[i][j] = ga[i][j] = 0.f;
+    for (int j = 0; j < 2; ++j) lA[i][j] = lB[i][j] = 0.f;
     if (i < nrows) {
       const int z = zb + i;
+      {
+        const float2 v = __ldg(reinterpret_cast<const float2*>(vel + i * NX));
+        sts2(V2o + i * NX, v.x * v.x * dt2, v.y * v.y * dt2);
+        sts2(GAo + i * NX, 0.0f, 0.0f);
+      }
 #pragma unroll
       for (int j = 0; j < 2; ++j) {
         const int cell = gbase + i * NX + j;
@@ -467,7 +478,7 @@ __global__ void __launch_bounds__(NSEG * 32 * (1 + NI), 1) adj3_kernel(const __g
         if (!p.first) {
           lA[i][j] = sLc[cell];
           lB[i][j] = sLp[cell];
-          ga[i][j] = gacc[i * NX + j];
+          GAo[i * NX + j] = gacc[i * NX + j];
           const int xx = x + j;
           if (xx < swa || xx >= NX - swa) {
             const int xc = strip_col(xx, NX, swa);
@@ -488,20 +499,21 @@ __global__ void __launch_bounds__(NSEG * 32 * (1 + NI), 1) adj3_kernel(const __g
 
   const int pr_lo = (rank > 0) ? split_row(nz, C, rank - 1) - FD_PAD : 0;
 
-  // Derived terms of this thread's cells for lambda `lc` into buffer b.
+  // Derived terms of this thread's cells for lambda `lc`: VS into buffer b, the strip terms into
+  // their single buffers.
   auto derive = [&](int b, const float (&lc)[S][2]) {
     float* VSb = sm + L.off_vs + b * vstride;
-    float* TXb = sm + L.off_tx + b * xstride + abase;
-    float* U1Xb = sm + L.off_u1x + b * xstride + abase;
-    float* TZb = sm + L.off_tz + b * zstride + zbase;
-    float* U1Zb = sm + L.off_u1z + b * zstride + zbase;
+    float* TXb = TXs;
+    float* U1Xb = U1Xs;
+    float* TZb = TZs;
+    float* U1Zb = U1Zs;
 #pragma unroll
     for (int i = 0; i < S; ++i) {
       if (i < nrows) {
         const int z = zb + i;
-        const float2 v = __ldg(reinterpret_cast<const float2*>(vel + i * NX));
-        const float vs0 = (v.x * v.x * dt2) * lc[i][0];
-        const float vs1 = (v.y * v.y * dt2) * lc[i][1];
+        const float2 v2 = lds2(V2o + i * NX);
+        const float vs0 = v2.x * lc[i][0];
+        const float vs1 = v2.y * lc[i][1];
         sts2(VSb + vbase + i * NX, vs0, vs1);
         if constexpr (C > 1) {
           if (rank > 0 && z < r0 + FD_PAD) st_peer_v2(VSb + (z - pr_lo) * NX + x, rank - 1, vs0, vs1);
@@ -548,10 +560,10 @@ __global__ void __launch_bounds__(NSEG * 32 * (1 + NI), 1) adj3_kernel(const __g
   auto step = [&](int t, float (&lc)[S][2], float (&lp)[S][2]) {
     const int par = (p.t_hi - 1 - t) & 1;
     const float* VSd = sm + L.off_vs + par * vstride + vbase;
-    const float* TXd = sm + L.off_tx + par * xstride + abase;
-    const float* U1Xd = sm + L.off_u1x + par * xstride + abase;
-    const float* TZd = sm + L.off_tz + par * zstride + zbase;
-    const float* U1Zd = sm + L.off_u1z + par * zstride + zbase;
+    const float* TXd = TXs;
+    const float* U1Xd = U1Xs;
+    const float* TZd = TZs;
+    const float* U1Zd = U1Zs;
     const float f = __ldg(&g.wavelet[t]);
     const float* res_t = p.residual + (static_cast<size_t>(unit) * nt + t) * nrec;
     const float* st_t = p.stored + (static_cast<size_t>(unit) * segn + (t - p.t_lo)) * cells + gbase;
@@ -637,13 +649,18 @@ __global__ void __launch_bounds__(NSEG * 32 * (1 + NI), 1) adj3_kernel(const __g
             if (cell + 1 == sc[k]) g1 = g1 + lc[i][1] * (((((-2.0f) * v.y) * dt2) * wk_) * f);
           }
         }
-        ga[i][0] = ga[i][0] + g0;
-        ga[i][1] = ga[i][1] + g1;
+        {
+          const float2 ga = lds2(GAo + i * NX);
+          sts2(GAo + i * NX, ga.x + g0, ga.y + g1);
+        }
         lp[i][0] = n0;
         lp[i][1] = n1;
       }
     }
-    if (t > p.t_lo) derive(1 - par, lp);
+    if (t > p.t_lo) {
+      __syncthreads();  // every read of the single-buffered strip terms of step t is done
+      derive(1 - par, lp);
+    }
     if constexpr (C > 1) {
       if (pusher) fence_cluster();
       __syncthreads();
@@ -679,7 +696,7 @@ __global__ void __launch_bounds__(NSEG * 32 * (1 + NI), 1) adj3_kernel(const __g
         const int cell = gbase + i * NX + j;
         sLc[cell] = flips ? lB[i][j] : lA[i][j];
         sLp[cell] = flips ? lA[i][j] : lB[i][j];
-        gacc[i * NX + j] = ga[i][j];
+        gacc[i * NX + j] = GAo[i * NX + j];
         const int xx = x + j;
         if (xx < swa || xx >= NX - swa) {
           const int xc = strip_col(xx, NX, swa);

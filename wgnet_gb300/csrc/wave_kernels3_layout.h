@@ -34,9 +34,12 @@ __host__ __device__ inline F3Layout f3_layout_rt(int NX, int pmlp, int nz, int s
 
 struct A3Layout {
   int maxrows, lr, zs;
-  int off_vs, off_tx, off_u1x, off_tz, off_u1z, off_lpx, off_lzx, off_lpz, off_lzz, off_prof, off_opb, total;
+  int off_vs, off_tx, off_u1x, off_tz, off_u1z, off_lpx, off_lzx, off_lpz, off_lzz, off_v2, off_ga, off_prof, off_opb,
+      total;
 };
 
+// VS is exchanged with the peer CTA and double-buffered; the x- and z-strip derived terms are read
+// only inside the CTA and are single-buffered (a CTA barrier separates their reads and writes).
 __host__ __device__ inline A3Layout a3_layout_rt(int NX, int pmlp, int nz, int swa, int C) {
   const int SW = g3_sw(pmlp);
   A3Layout L;
@@ -45,15 +48,17 @@ __host__ __device__ inline A3Layout a3_layout_rt(int NX, int pmlp, int nz, int s
   L.zs = (C == 1 ? 2 : 1) * swa;
   const int sx = L.maxrows * 2 * SW, sz = L.zs * NX;
   L.off_vs = 0;                           // VS[2][lr][NX]   v^2 dt^2 lambda
-  L.off_tx = L.off_vs + 2 * L.lr * NX;    // TX[2][maxrows][2 SW]
-  L.off_u1x = L.off_tx + 2 * sx;          // U1X[2][maxrows][2 SW]
-  L.off_tz = L.off_u1x + 2 * sx;          // TZ[2][zs][NX]
-  L.off_u1z = L.off_tz + 2 * sz;          // U1Z[2][zs][NX]
-  L.off_lpx = L.off_u1z + 2 * sz;         // LPX[maxrows][2 SW]  adjoint psi_x (owner only)
+  L.off_tx = L.off_vs + 2 * L.lr * NX;    // TX[maxrows][2 SW]
+  L.off_u1x = L.off_tx + sx;              // U1X[maxrows][2 SW]
+  L.off_tz = L.off_u1x + sx;              // TZ[zs][NX]
+  L.off_u1z = L.off_tz + sz;              // U1Z[zs][NX]
+  L.off_lpx = L.off_u1z + sz;             // LPX[maxrows][2 SW]  adjoint psi_x (owner only)
   L.off_lzx = L.off_lpx + sx;             // LZX[maxrows][2 SW]  adjoint zeta_x
   L.off_lpz = L.off_lzx + sx;             // LPZ[zs][NX]
   L.off_lzz = L.off_lpz + sz;             // LZZ[zs][NX]
-  L.off_prof = L.off_lzz + sz;            // ax bx dbx az bz dbz
+  L.off_v2 = L.off_lzz + sz;              // V2[maxrows][NX]     v^2 dt^2 (owner only)
+  L.off_ga = L.off_v2 + L.maxrows * NX;   // GA[maxrows][NX]     gradient accumulator (owner only)
+  L.off_prof = L.off_ga + L.maxrows * NX; // ax bx dbx az bz dbz
   L.off_opb = L.off_prof + 3 * (NX + nz); // 1 + bx, per column
   L.total = (L.off_opb + NX + 3) & ~3;
   return L;
