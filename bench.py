@@ -42,6 +42,9 @@ PML = 20
 CK = 50
 UPDATED_CELLS = (NX + 2 * (PML + 2) - 4) ** 2  # 110 x 110 cells updated per step
 FLOPS_PER_CELL_UPDATE = 48.0  # average over interior / one-PML-axis / two-PML-axes cells at pml 20
+# DRAM bytes per (unit, step) measured with ncu on the small case (32 models, nt 200) and scaled by
+# unit-steps to a full launch: profiles/adj3_kernel_b32_nt200.md, fwd3_kernel_recompute_b32_nt200.md
+MEASURED_TRAFFIC_PER_UNIT_STEP = {"adjoint": 445.93e6 / 8000 + 9.22e6 / 8000, "recompute": (65.0e6 + 341.1e6) / 8000}
 
 
 def clocks_sampler(stop: threading.Event, out: list):
@@ -283,7 +286,8 @@ def main():
         "gpu_launches": launches,
         "kernels_ms": {names[k]: {"total_ms": kms[k], "launches": int(kn[k])} for k in range(3)},
         "roofline": {"kernel": names[dom], "bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-                     "frac": achieved / hbm_peak, "traffic": None, "peak_source": peak_kind,
+                     "frac": achieved / hbm_peak, "peak_source": peak_kind,
+                     "traffic": (MEASURED_TRAFFIC_PER_UNIT_STEP.get(names[dom], 0.0) * units * steps_per_launch) or None,
                      "bytes_per_launch": per, "avg_launch_ms": avg_ms},
         "roofline_fp32": {"kernel": names[dom], "achieved_tflops": fp32_tflops,
                           "flops_per_launch": flops_launch, "flops_per_cell_update": FLOPS_PER_CELL_UPDATE},
