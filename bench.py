@@ -144,6 +144,154 @@ def run_reference(args):
     return 0
 
 
+DATAGEN_METRIC = "gathers/s (batched forward data generation, 70/100/140 grids, 5 shots, nt=1000, FP16 x4-decimated)"
+DATAGEN_UNIT = "gathers/s"
+
+
+def run_datagen(args):
+    """Batched data generation: `args.models` seeded mixed-family models, grids 70/100/140 round-robin,
+    5 shots, nt = 1000, dt = 1 ms, simulated, low-passed and decimated to FP16 [N, 5, 250, n] by one
+    CUDA graph launch per step."""
+    import torch
+
+    from wgnet_gb300 import _lib
+    from wgnet_gb300.datagen import GatherGenerator, round_robin_counts, synthetic_batch
+
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    total = args.models
+    counts = round_robin_counts(total)
+    batch = synthetic_batch(total, seed=0)
+    gen = GatherGenerator(counts, nt=args.nt)
+    gen.run(batch)
+    torch.cuda.synchronize()
+    for _ in range(args.warmup):
+        gen.launch()
+    torch.cuda.synchronize()
+    stop = threading.Event()
+    clk = []
+    th = threading.Thread(target=clocks_sampler, args=(stop, clk), daemon=True)
+    th.start()
+    time.sleep(0.3)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record()
+    for _ in range(args.steps):
+        gen.launch()
+    ev1.record()
+    torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1)
+    stop.set()
+    th.join(timeout=2)
+    value = total * args.steps / (ms / 1000.0)
+    # e2e: pinned host velocities -> device, graph, FP16 gathers -> pinned host
+    h_in = {n: torch.from_numpy(v).pin_memory() for n, v in batch.items()}
+    h_out = {n: torch.empty(g.shape, dtype=g.dtype).pin_memory() for n, g in gen.gathers.items()}
+
+    def host_step():
+        gen.load(h_in)
+        gen.launch()
+        for n, g in gen.gathers.items():
+            h_out[n].copy_(g, non_blocking=True)
+        torch.cuda.synchronize()
+
+    host_step()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        host_step()
+    e2e_s = time.perf_counter() - t0
+    e2e = total * args.steps / e2e_s
+    h2d = sum(t.numel() * 4 for t in h_in.values())
+    d2h = sum(t.numel() * 2 for t in h_out.values())
+    ok = all(torch.isfinite(h_out[n].float()).all().item() for n in h_out)
+    # per-grid forward kernel time, measured eagerly with the engine's event timer on the same batch
+    per_grid = {}
+    flops = 0.0
+    for n, eng in gen.engines.items():
+        d = torch.from_numpy(batch[n]).cuda()
+        eng.simulate_torch(d)
+        torch.cuda.synchronize()
+        eng.profile(True)
+        eng.simulate_torch(d)
+        torch.cuda.synchronize()
+        fms, fl = eng.profile_read()["forward"]
+        eng.profile(False)
+        upd = (eng.nx - 4) * (eng.nz - 4)
+        f = counts[n] * SHOTS * args.nt * upd * FLOPS_PER_CELL_UPDATE
+        flops += f
+        per_grid[str(n)] = {"models": counts[n], "forward_ms": fms, "launches": fl, "launch_shape": gen.shapes[n],
+                            "gcell_updates_per_s": counts[n] * SHOTS * args.nt * upd / (fms / 1000.0) / 1e9}
+    dom = max(per_grid, key=lambda k: per_grid[k]["forward_ms"])
+    dn = int(dom)
+    dom_ms = per_grid[dom]["forward_ms"]
+    dom_bytes = counts[dn] * SHOTS * (args.nt * dn * 4 + (dn + 44) ** 2 * 4)
+    hbm_peak, peak_kind = measured_peaks()
+    props = torch.cuda.get_device_properties(0)
+    line = {
+        "metric": DATAGEN_METRIC, "value": value, "unit": DATAGEN_UNIT, "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32 (FP16 output)", "data": "synthetic (seeded mixed-family models)",
+        "config": {"workload": f"config 2 batched generation: {total} models round-robin over 70x70/100x100/140x140, "
+                               f"5 shots, nt={args.nt}, dt=1ms, low-pass + x4 decimation to FP16, one CUDA graph launch",
+                   "counts": counts, "l2": "inputs and outputs larger than L2 (f32 traces ~8 GB per step)",
+                   "kernels_per_graph": gen.kernels_per_launch},
+        "e2e": {"value": e2e, "unit": DATAGEN_UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "gpu_launches": gen.kernels_per_launch * args.steps, "outputs_finite": ok,
+        "per_grid": per_grid,
+        "roofline": {"kernel": f"forward {dom}x{dom}", "bound": "hbm",
+                     "achieved": dom_bytes / (dom_ms / 1000.0) / 1e9, "peak": hbm_peak, "unit": "GB/s",
+                     "frac": dom_bytes / (dom_ms / 1000.0) / 1e9 / hbm_peak, "peak_source": peak_kind,
+                     "traffic": None, "bytes_per_launch": dom_bytes, "avg_launch_ms": dom_ms},
+        "roofline_fp32": {"achieved_tflops": flops / (ms / args.steps / 1000.0) / 1e12,
+                          "sms": props.multi_processor_count},
+        "clocks": summarize_clocks(clk),
+    }
+    if not args.no_cpu_baseline:
+        from oracle import native as o
+
+        cores = o.cpu_threads()
+        sample = synthetic_batch(3 * max(1, cores // 3), seed=0)
+        t0 = time.perf_counter()
+        m = 0
+        for n, v in sample.items():
+            sv = o.Survey(shots=SHOTS, nt=args.nt, dt=DT, pml=PML, nx_vis=n, nz_vis=n)
+            o.forward(sv, v, sv.default_sources(), o.ricker(args.nt, DT, 15.0), threads=cores)
+            m += len(v)
+        secs = time.perf_counter() - t0
+        line["cpu_baseline"] = {"value": m / secs, "unit": DATAGEN_UNIT, "cores": cores, "kind": "port",
+                                "sample": f"{m} models of the mix ({secs:.1f} s), forward only, one shot per thread"}
+    print(json.dumps(line), flush=True)
+    gen.close()
+    return 0
+
+
+def run_reference_datagen(args):
+    """The reference's CPU forward (C++ restatement) on a bounded sample of the generation mix."""
+    from oracle import native as o
+    from wgnet_gb300.datagen import synthetic_batch
+
+    cores = o.cpu_threads()
+    sample = synthetic_batch(3 * max(1, cores // 3), seed=0)
+    times = []
+    m = sum(len(v) for v in sample.values())
+    for i in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        for n, v in sample.items():
+            sv = o.Survey(shots=SHOTS, nt=args.nt, dt=DT, pml=PML, nx_vis=n, nz_vis=n)
+            o.forward(sv, v, sv.default_sources(), o.ricker(args.nt, DT, 15.0), threads=cores)
+        if i >= args.warmup:
+            times.append(time.perf_counter() - t0)
+    value = m * len(times) / sum(times)
+    print(json.dumps({"impl": "reference", "metric": DATAGEN_METRIC, "value": value, "unit": DATAGEN_UNIT,
+                      "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+                      "ms_per_step": 1000.0 * sum(times) / len(times), "higher_is_better": True, "scaling": "weak",
+                      "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+                      "config": {"workload": f"{m} models of the 70/100/140 mix (bounded sample), forward only"},
+                      "cpu_baseline": {"value": value, "unit": DATAGEN_UNIT, "cores": cores, "kind": "port",
+                                       "sample": f"{m} models per step"},
+                      "e2e": {"value": value, "unit": DATAGEN_UNIT, "h2d_bytes_per_step": 0,
+                              "d2h_bytes_per_step": 0}}), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -154,7 +302,15 @@ def main():
     ap.add_argument("--checkpoint", type=int, default=CK)
     ap.add_argument("--nt", type=int, default=NT, help="time steps (profiling runs use a short record)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", default="gradient", choices=["gradient", "datagen"],
+                    help="gradient: the 256-model misfit-gradient batch (default); datagen: batched generation")
     args = ap.parse_args()
+    if args.workload == "datagen":
+        if args.models == MODELS:
+            args.models = 4096
+        if args.impl == "reference":
+            return run_reference_datagen(args)
+        return run_datagen(args)
     if args.impl == "reference":
         return run_reference(args)
     nt = args.nt

@@ -12,6 +12,8 @@
 #ifndef WGNET_GB300_H
 #define WGNET_GB300_H
 
+#include <stddef.h>
+
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -110,6 +112,37 @@ int wg_cpml_profiles(int n, float h, float dt, int width, float max_vel, float f
  * `series` blocks of [nt][nrec] traces, zero history before t = 0. Device pointers. */
 int wg_bandlimit_dev(const float* d_in, const float* d_kernel, int klen, int series, int nt, int nrec, float* d_out,
                      void* stream);
+
+/* Wave-cache writer step (python/wgnet/data.py:138-179, which decimates by plain subsampling
+ * `[:, ::8, :]` and stores float16): zero-phase FIR low-pass (taps d_kernel[0..klen), centre tap
+ * `center`) then decimation by `factor`, [series][nt][nrec] f32 -> [series][ceil(nt/factor)][nrec]
+ * IEEE half. Device pointers. */
+int wg_lowpass_decimate_f16_dev(const float* d_in, const float* d_kernel, int klen, int center, int factor, int series,
+                                int nt, int nrec, void* d_out, void* stream);
+
+/* Batched forward data generation (the wave-cache writer, python/wgnet/data.py:138-179, for many
+ * models and several grid sizes at once). Group i simulates models[i] models with engines[i]
+ * (velocities d_vel[i], [models][nz_vis][nx_vis] m/s, device) and writes low-passed, decimated
+ * IEEE-half gathers to d_out[i], [models][shots][ceil(nt/factor)][nrec] (device). The low-pass is
+ * the FIR `taps` (host, odd length klen, applied zero-phase about the centre tap) or, when taps is
+ * NULL, physics.py's Gaussian lowpass_kernel with its -3 dB point at cutoff_hz (0: 0.4 x the
+ * decimated Nyquist frequency; factor 1 with cutoff 0 is a plain cast). The work of all groups is
+ * captured into one CUDA graph, one branch per group, at creation: buffers and engine statics are
+ * fixed then, and wg_gen_plan_launch replays it on `stream` (NULL = default stream). Engines must
+ * outlive the plan and share dt. workspace_bytes bounds the f32 trace workspace (0: 16 GiB);
+ * larger batches are processed in chunks inside the graph. */
+typedef struct wg_gen_plan wg_gen_plan;
+int wg_gen_plan_create(wg_engine* const* engines, const int* models, int groups, const float* const* d_vel,
+                       void* const* d_out, int factor, const float* taps, int klen, float cutoff_hz,
+                       size_t workspace_bytes, wg_gen_plan** out);
+int wg_gen_plan_launch(wg_gen_plan* plan, void* stream);
+/* Kernels per launch, trace workspace bytes, and the filter taps (up to taps_cap of *klen). */
+int wg_gen_plan_info(const wg_gen_plan* plan, int* kernels, size_t* trace_bytes, float* taps, int taps_cap, int* klen);
+void wg_gen_plan_destroy(wg_gen_plan* plan);
+/* lowpass_kernel (python/wgnet/physics.py:18-26) on the host, with the C library's exp (which may
+ * differ from numpy's in the last bit of a tap): returns the tap count n and writes the taps when
+ * out != NULL and cap >= n; negative status on bad arguments. */
+int wg_lowpass_taps(double fmax_hz, double dt, float* out, int cap);
 
 /* render_residual (python/wgnet/render.py:86-109): activated slot parameters [B][1225][6] ->
  * residual field [B][70][70] in km/s; and its vector-Jacobian product: cotangent [B][70][70] ->

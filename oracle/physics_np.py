@@ -35,3 +35,20 @@ def bandlimit(traces: np.ndarray, kernel: np.ndarray) -> np.ndarray:
             continue
         y[..., lag:, :] += k[j] * x[..., : nt - lag, :]
     return y
+
+
+def lowpass_decimate_f16(traces: np.ndarray, taps: np.ndarray, center: int, factor: int) -> np.ndarray:
+    """Wave-cache writer step (python/wgnet/data.py:163-166 subsamples `[:, ::factor, :]` and casts
+    to float16): here a zero-phase FIR first, y[j] = sum_k taps[k] x[j factor + k - center] (zero
+    outside [0, nt)), accumulated in f32 over k in increasing order, then rounded to float16
+    (round to nearest even). `traces` is [..., nt, nrec]; returns [..., ceil(nt / factor), nrec]."""
+    x = np.asarray(traces, np.float32)
+    nt = x.shape[-2]
+    nt_out = -(-nt // factor)
+    acc = np.zeros(x.shape[:-2] + (nt_out, x.shape[-1]), np.float32)
+    j = np.arange(nt_out)
+    for k, w in enumerate(np.asarray(taps, np.float32)):
+        t = j * factor + k - center
+        ok = (t >= 0) & (t < nt)
+        acc[..., ok, :] = acc[..., ok, :] + w * x[..., t[ok], :]
+    return acc.astype(np.float16)

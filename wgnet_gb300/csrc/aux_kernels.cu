@@ -1,6 +1,7 @@
 // Small kernels around the time-stepping kernels: velocity padding, observed energy, residual and
 // misfit, gradient shot-sum/mask/fold, causal band-limit FIR. All are HBM-bound elementwise or
 // reduction passes; reductions use a fixed launch shape and a fixed tree so they are deterministic.
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -121,6 +122,25 @@ __global__ void bandlimit_kernel(const float* __restrict__ in, const float* __re
   out[(static_cast<size_t>(s) * nt + t) * nrec + r] = acc;
 }
 
+// Zero-phase FIR low-pass and decimation to FP16: out[s][j][r] = sum_k ker[k] in[s][j*factor + k -
+// center][r] (zero outside [0, nt)), for j < nt_out. One thread per output sample; the series' time
+// window is read through L1.
+__global__ void decimate_kernel(const float* __restrict__ in, const float* __restrict__ ker, int klen, int center,
+                                int factor, int nt, int nrec, int nt_out, __half* __restrict__ out) {
+  const int s = blockIdx.z;
+  const int j = blockIdx.y;
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= nrec) return;
+  const float* x = in + static_cast<size_t>(s) * nt * nrec + r;
+  const int t0 = j * factor - center;
+  float acc = 0.0f;
+  for (int k = 0; k < klen; ++k) {
+    const int t = t0 + k;
+    if (t >= 0 && t < nt) acc = acc + __ldg(&ker[k]) * __ldg(&x[static_cast<size_t>(t) * nrec]);
+  }
+  out[(static_cast<size_t>(s) * nt_out + j) * nrec + r] = __float2half_rn(acc);
+}
+
 __global__ void scale_kernel(const float* __restrict__ in, float alpha, size_t n, float* __restrict__ out) {
   for (size_t i = blockIdx.x * static_cast<size_t>(blockDim.x) + threadIdx.x; i < n;
        i += static_cast<size_t>(gridDim.x) * blockDim.x)
@@ -160,6 +180,13 @@ cudaError_t launch_bandlimit(const float* in, const float* ker, int klen, int se
                              cudaStream_t s) {
   dim3 grid((nrec + 127) / 128, nt, series);
   bandlimit_kernel<<<grid, 128, 0, s>>>(in, ker, klen, nt, nrec, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_decimate(const float* in, const float* ker, int klen, int center, int factor, int series, int nt,
+                            int nrec, int nt_out, void* out_half, cudaStream_t s) {
+  dim3 grid((nrec + 63) / 64, nt_out, series);
+  decimate_kernel<<<grid, 64, 0, s>>>(in, ker, klen, center, factor, nt, nrec, nt_out, static_cast<__half*>(out_half));
   return cudaGetLastError();
 }
 

@@ -144,6 +144,8 @@ struct wg_engine {
   wg::Shape fshape{0, 0, 0}, ashape{0, 0, 0};
   int ck_every = 50;
   int adj_prefetch = 1;
+  int streamed = 0;  // 1: wavefields in HBM, one launch per step (grids beyond the resident kernels)
+  wg::StreamWork* sw = nullptr;
   // per-kernel timing: (kind, start, stop) events recorded on the launching stream
   bool prof_on = false;
   std::vector<int> prof_kind;
@@ -187,6 +189,30 @@ struct wg_engine {
 };
 
 namespace {
+
+// The engine's device statics and launch settings (the caller holds the engine's lock).
+wg::EngineView view_of(const wg_engine* e) {
+  wg::EngineView v;
+  v.grid = e->grid();
+  v.stations = e->stations();
+  v.shots = e->shots;
+  v.nt = e->nt;
+  v.nrec = e->nrec;
+  v.nx = e->nx;
+  v.nz = e->nz;
+  v.nx_vis = e->nx_vis;
+  v.nz_vis = e->nz_vis;
+  v.pad = e->pad;
+  v.ck_every = e->ck_every;
+  v.vmin = e->cfg.vmin;
+  v.vmax = e->cfg.vmax;
+  v.dt = e->cfg.dt;
+  v.fshape = e->fshape;
+  v.ashape = e->ashape;
+  v.d_status = e->d_status.as<int>();
+  v.adj_prefetch = e->adj_prefetch;
+  return v;
+}
 
 // Bilinear corners of a station (wave_wgpu.rs:217-230): x0 = min(floor(gx), nx - 2).
 void corners(const wg_engine& e, float px, float pz, int* cell, float* w) {
@@ -280,10 +306,10 @@ bool find_shape(int which, int cluster, int threads, int cpt, wg::Shape* out) {
 bool pick_shapes(wg_engine* e) {
   // Preference order; the first compiled shape that fits the grid is the default (the autotuner
   // can choose another among wg_shape_candidates).
-  static const int fpref[][3] = {{2, 704, 10}, {2, 896, 8}, {4, 896, 4}, {4, 448, 8}, {1, 1024, 12},
+  static const int fpref[][3] = {{2, 704, 10}, {4, 672, 10}, {6, 640, 12}, {2, 896, 8}, {4, 480, 14}, {6, 384, 20}, {4, 896, 4}, {4, 448, 8}, {1, 1024, 12},
                                  {2, 1024, 6}, {2, 512, 12}, {2, 1024, 10}, {4, 1024, 8}, {2, 1024, 16},
                                  {4, 512, 16}};
-  static const int apref[][3] = {{2, 704, 10}, {2, 896, 8}, {2, 1024, 6}, {4, 896, 4}, {4, 448, 8},
+  static const int apref[][3] = {{2, 704, 10}, {4, 672, 10}, {6, 640, 12}, {2, 896, 8}, {4, 480, 14}, {6, 384, 20}, {2, 1024, 6}, {4, 896, 4}, {4, 448, 8},
                                  {2, 512, 12}, {4, 1024, 4}, {4, 1024, 8}, {4, 512, 16}};
   e->fshape = wg::Shape{0, 0, 0};
   e->ashape = wg::Shape{0, 0, 0};
@@ -567,30 +593,13 @@ int read_status(wg_engine* e) {
 }  // namespace
 
 namespace wg {
+using ::view_of;
 
 // Snapshot of the engine's statics under its lock; `lock` keeps the engine locked while the caller
 // launches with them.
 EngineView engine_view(wg_engine* e, std::unique_lock<std::mutex>& lock) {
   lock = std::unique_lock<std::mutex>(e->mu);
-  EngineView v;
-  v.grid = e->grid();
-  v.stations = e->stations();
-  v.shots = e->shots;
-  v.nt = e->nt;
-  v.nrec = e->nrec;
-  v.nx = e->nx;
-  v.nz = e->nz;
-  v.nx_vis = e->nx_vis;
-  v.nz_vis = e->nz_vis;
-  v.pad = e->pad;
-  v.ck_every = e->ck_every;
-  v.vmin = e->cfg.vmin;
-  v.vmax = e->cfg.vmax;
-  v.fshape = e->fshape;
-  v.ashape = e->ashape;
-  v.d_status = e->d_status.as<int>();
-  v.adj_prefetch = e->adj_prefetch;
-  return v;
+  return view_of(e);
 }
 
 int engine_device(const wg_engine* e) { return e->device; }
@@ -864,6 +873,19 @@ int wg_bandlimit_dev(const float* d_in, const float* d_kernel, int klen, int ser
   if (series == 0 || nt == 0 || nrec == 0) return WG_OK;
   if (d_in == d_out) return fail(WG_ERR_ARG, "bandlimit cannot run in place");
   WG_LAUNCH(wg::launch_bandlimit(d_in, d_kernel, klen, series, nt, nrec, d_out, static_cast<cudaStream_t>(stream)));
+  return WG_OK;
+}
+
+int wg_lowpass_decimate_f16_dev(const float* d_in, const float* d_kernel, int klen, int center, int factor, int series,
+                                int nt, int nrec, void* d_out, void* stream) {
+  if (!d_in || !d_kernel || !d_out || klen < 1 || center < 0 || center >= klen || factor < 1 || series < 0 || nt < 0 ||
+      nrec < 0)
+    return fail(WG_ERR_ARG, "bad argument");
+  const int nt_out = (nt + factor - 1) / factor;
+  if (series == 0 || nt_out == 0 || nrec == 0) return WG_OK;
+  if (nt_out > 65535) return fail(WG_ERR_ARG, "too many output samples");
+  WG_LAUNCH(wg::launch_decimate(d_in, d_kernel, klen, center, factor, series, nt, nrec, nt_out, d_out,
+                                static_cast<cudaStream_t>(stream)));
   return WG_OK;
 }
 

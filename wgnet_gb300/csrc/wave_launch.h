@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 
 #include <cstddef>
+#include <string>
 
 #include "wave_common.cuh"
 
@@ -60,6 +61,11 @@ cudaError_t launch_fold(const float* gacc, const float* mask, int models, int sh
 cudaError_t launch_bandlimit(const float* in, const float* ker, int klen, int series, int nt, int nrec, float* out,
                              cudaStream_t s);
 
+// Zero-phase FIR (taps ker[0..klen), centre tap `center`) and decimation by `factor` of
+// [series][nt][nrec] traces into FP16 [series][nt_out][nrec].
+cudaError_t launch_decimate(const float* in, const float* ker, int klen, int center, int factor, int series, int nt,
+                            int nrec, int nt_out, void* out_half, cudaStream_t s);
+
 // Error reporting and launch accounting shared by the C ABI entry points (engine.cu).
 int report_error(int code, const char* msg);
 void note_launch();
@@ -70,11 +76,31 @@ struct EngineView {
   Grid grid;
   Stations stations;
   int shots, nt, nrec, nx, nz, nx_vis, nz_vis, pad, ck_every;
-  float vmin, vmax;
+  float vmin, vmax, dt;
   Shape fshape, ashape;
   int* d_status;
   int adj_prefetch;
 };
+
+// Event marks around groups of launches (kind 0 forward, 1 forward recompute, 2 adjoint) for the
+// engine's per-kernel timing; no-op without a callback.
+struct StreamTimer {
+  void* ctx = nullptr;
+  void (*fn)(void* ctx, int kind, bool begin, cudaStream_t s) = nullptr;
+  void mark(int kind, bool begin, cudaStream_t s) const {
+    if (fn) fn(ctx, kind, begin, s);
+  }
+};
+
+// Streamed path (stream.cu): wavefields in HBM, one persistent TMA-pipelined launch per time step.
+struct StreamWork;
+StreamWork* stream_work_new();
+void stream_work_free(StreamWork* w);
+bool stream_supported(const EngineView& v, std::string* why);
+int stream_simulate(StreamWork* w, const EngineView& v, const int* h_rec_cell, const float* d_vis, int models,
+                    float* d_traces, cudaStream_t st, const StreamTimer& timer);
+int stream_gradient(StreamWork* w, const EngineView& v, const int* h_rec_cell, const float* d_vis, const float* d_obs,
+                    int models, double* d_loss, float* d_grad, cudaStream_t st, const StreamTimer& timer);
 
 // out[i] = in[i] * alpha (unit conversion), n elements.
 cudaError_t launch_scale(const float* in, float alpha, size_t n, float* out, cudaStream_t s);

@@ -25,7 +25,11 @@ namespace wg {
   X(114, 12, 2, 4, 14, 1)       \
   X(114, 12, 4, 4, 7, 1)        \
   X(114, 12, 4, 2, 14, 1)       \
-  X(114, 12, 1, 8, 14, 1)
+  X(114, 12, 1, 8, 14, 1)       \
+  X(144, 12, 4, 5, 7, 2)        \
+  X(144, 12, 4, 7, 5, 2)        \
+  X(184, 12, 6, 6, 5, 3)        \
+  X(184, 12, 6, 10, 3, 3)
 
 #define WG_ADJ_SHAPES(X) \
   X(2, 1024, 6)          \

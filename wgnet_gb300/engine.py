@@ -114,6 +114,18 @@ class WaveEngine:
             check(-n)
         return [tuple(int(v) for v in buf[3 * i:3 * i + 3]) for i in range(min(n, 64))]
 
+    def profile(self, enable: bool = True) -> None:
+        """Start (clearing earlier records) or stop per-kernel event timing."""
+        check(self._lib.wg_profile(self._h, int(bool(enable))))
+
+    def profile_read(self) -> dict[str, tuple[float, int]]:
+        """{kind: (milliseconds, launches)} since profile(True), for the forward, forward-recompute,
+        adjoint and auxiliary kernels; clears the records."""
+        ms = np.zeros(4, np.float64)
+        n = np.zeros(4, np.int64)
+        check(self._lib.wg_profile_read(self._h, ptr(ms), ptr(n), 4))
+        return {k: (float(ms[i]), int(n[i])) for i, k in enumerate(("forward", "recompute", "adjoint", "aux"))}
+
     # -- host (numpy) entry points -----------------------------------------------------------
     def _vel(self, vel_mps) -> np.ndarray:
         v = np.ascontiguousarray(vel_mps, dtype=np.float32)
