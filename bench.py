@@ -263,6 +263,165 @@ def run_datagen(args):
     return 0
 
 
+LARGE_METRIC = "Gcell-updates/s (forward + exact adjoint, 800x300 at 5 m, 40 shots, nt=4000, streamed)"
+LARGE_UNIT = "Gcell-updates/s"
+
+
+def large_workload(nt: int, shots: int = 40):
+    """One 800 x 300 model (5 m cells: padded 844 x 344), dt = 0.5 ms, `shots` evenly spaced surface
+    shots, 800 receivers; observed data from the true layered/curved/faulted/blob model, gradient
+    at its 5-cell smoothed version."""
+    from wgnet_gb300 import models_synth
+
+    true = models_synth.make_batch(1, seed=4, nz=300, nx=800, families=("fault",))
+    start = models_synth.smooth(true, 5.0)
+    return true, start
+
+
+def large_bytes_per_cell_update(nx: int, nz: int, pml: int, shots: int) -> tuple[float, float]:
+    """Algorithmic DRAM bytes per updated cell and step of the streamed forward (with stored
+    gradient terms) and adjoint kernels: wavefield reads/writes, stored terms, gradient
+    accumulator, velocity (shared by the shots), and 16 B per C-PML axis (psi and zeta)."""
+    region = pml + 6
+    fx = 2 * (region - 2) / (nx - 4)
+    fz = 2 * (region - 2) / (nz - 4)
+    pml_b = 16.0 * (fx + fz)
+    fwd = 4 + 4 + 4 + 4 / shots + 4 + pml_b          # u, u_prev, u_next, v, stored
+    adj = 4 + 8 + 4 + 8 + 4 / shots + pml_b          # lambda, lambda_prev r/w, stored, gacc r/w, v
+    return fwd, adj
+
+
+def run_large(args):
+    import torch
+
+    from wgnet_gb300 import _lib
+    from wgnet_gb300.engine import WaveEngine
+
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    nt, shots = args.nt, args.shots
+    true, start = large_workload(nt, shots)
+    eng = WaveEngine(shots=shots, nt=nt, dt=0.0005, peak_hz=15.0, pml=PML, vmin=1000.0, vmax=5000.0, nx_vis=800,
+                     nz_vis=300, h=5.0)
+    assert eng.get_option("streamed") == 1
+    dev = torch.device("cuda", torch.cuda.current_device())
+    d_true = torch.from_numpy(true).to(dev)
+    d_obs = eng.simulate_torch(d_true)
+    d_start = torch.from_numpy(start).to(dev)
+    for _ in range(args.warmup):
+        eng.evaluate_adjoint_torch(d_start, d_obs)
+    torch.cuda.synchronize()
+    stop = threading.Event()
+    clk = []
+    th = threading.Thread(target=clocks_sampler, args=(stop, clk), daemon=True)
+    th.start()
+    time.sleep(0.3)
+    eng.profile(True)
+    _lib.launch_count(reset=True)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record()
+    for _ in range(args.steps):
+        loss, grad = eng.evaluate_adjoint_torch(d_start, d_obs)
+    ev1.record()
+    torch.cuda.synchronize()
+    launches = _lib.launch_count()
+    ms = ev0.elapsed_time(ev1)
+    prof = eng.profile_read()
+    eng.profile(False)
+    stop.set()
+    th.join(timeout=2)
+    assert torch.isfinite(loss).all() and torch.isfinite(grad).all()
+    upd = (eng.nx - 4) * (eng.nz - 4)
+    cell_updates = 2.0 * upd * nt * shots  # forward + adjoint per gradient
+    value = cell_updates * args.steps / (ms / 1000.0) / 1e9
+    # e2e: host velocity and observed data in, loss and gradient out, through the C ABI host entry
+    h_vel = torch.from_numpy(start).pin_memory()
+    h_obs = d_obs.cpu().pin_memory()
+    h_loss = torch.empty(1, dtype=torch.float64).pin_memory()
+    h_grad = torch.empty((1, 300, 800), dtype=torch.float32).pin_memory()
+    lib = _lib.load()
+
+    def host_step():
+        _lib.check(lib.wg_evaluate_adjoint(eng._h, h_vel.data_ptr(), h_obs.data_ptr(), 1, h_loss.data_ptr(),
+                                           h_grad.data_ptr()))
+
+    host_step()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        host_step()
+    e2e_s = time.perf_counter() - t0
+    e2e = cell_updates * args.steps / e2e_s / 1e9
+    bf, ba = large_bytes_per_cell_update(eng.nx, eng.nz, PML, shots)
+    fms, fn = prof["forward"]
+    ams, an = prof["adjoint"]
+    per_launch = upd * shots  # cell-updates per step launch
+    dom, dms, dbytes = ("adjoint", ams / max(an, 1) / nt, ba) if ams >= fms else ("forward", fms / max(fn, 1) / nt, bf)
+    achieved = per_launch * dbytes / (dms / 1000.0) / 1e9
+    hbm_peak, peak_kind = measured_peaks()
+    line = {
+        "metric": LARGE_METRIC, "value": value, "unit": LARGE_UNIT, "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded faulted layered model, smoothed start)",
+        "config": {"workload": f"config 4 large survey: 800x300 cells at 5 m (padded 844x344), {shots} shots, "
+                               f"800 receivers, dt=0.5ms, nt={nt}, forward + exact adjoint gradient, streamed path",
+                   "checkpointing": "every step's gradient term stored in HBM when it fits (auto)",
+                   "l2": "inputs larger than L2 (wavefields ~93 MB + stored terms ~186 GB per gradient)"},
+        "gradients_per_s": args.steps / (ms / 1000.0),
+        "e2e": {"value": e2e, "unit": LARGE_UNIT, "h2d_bytes_per_step": h_vel.numel() * 4 + h_obs.numel() * 4,
+                "d2h_bytes_per_step": 8 + h_grad.numel() * 4},
+        "gpu_launches": launches,
+        "kernels_ms": {"forward": {"total_ms": fms, "steps": nt * max(fn, 1)},
+                       "adjoint": {"total_ms": ams, "steps": nt * max(an, 1)}},
+        "roofline": {"kernel": f"{dom} step", "bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                     "frac": achieved / hbm_peak, "peak_source": peak_kind, "traffic": None,
+                     "bytes_per_cell_update": {"forward": bf, "adjoint": ba}, "avg_launch_ms": dms,
+                     "bytes_per_launch": per_launch * dbytes},
+        "clocks": summarize_clocks(clk),
+    }
+    if not args.no_cpu_baseline:
+        v, cores, sample = large_cpu_rate(true, start)
+        line["cpu_baseline"] = {"value": v, "unit": LARGE_UNIT, "cores": cores, "kind": "port", "sample": sample}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def large_cpu_rate(true, start, nt_sample: int = 400):
+    """The oracle's forward + adjoint (store-all, f32) of one shot per host thread over a 400-step
+    record of the large survey (the rate per cell-update does not depend on the record length)."""
+    from oracle import native as o
+
+    cores = o.cpu_threads()
+    sv = o.Survey(shots=cores, nt=nt_sample, dt=0.0005, h=5.0, nx_vis=800, nz_vis=300, pml=PML)
+    src = sv.default_sources()
+    wav = o.ricker(nt_sample, 0.0005, 15.0)
+    obs = o.forward(sv, true, src, wav, threads=cores)
+    t0 = time.perf_counter()
+    o.evaluate_adjoint(sv, start, src, wav, obs, threads=cores)
+    secs = time.perf_counter() - t0
+    upd = (sv.nx - 4) * (sv.nz - 4)
+    return (2.0 * upd * nt_sample * cores / secs / 1e9, cores,
+            f"{cores} shots x {nt_sample} steps of the survey ({secs:.1f} s), forward + adjoint, one shot per thread")
+
+
+def run_reference_large(args):
+    """The reference's CPU solver path (C++ restatement) on a bounded sample of the large survey."""
+    true, start = large_workload(args.nt, args.shots)
+    times = []
+    for i in range(args.warmup + args.steps):
+        v, cores, sample = large_cpu_rate(true, start)
+        if i >= args.warmup:
+            times.append(v)
+    value = sum(times) / len(times)
+    print(json.dumps({"impl": "reference", "metric": LARGE_METRIC, "value": value, "unit": LARGE_UNIT,
+                      "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": None,
+                      "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+                      "data": "synthetic", "config": {"workload": sample},
+                      "cpu_baseline": {"value": value, "unit": LARGE_UNIT, "cores": cores, "kind": "port",
+                                       "sample": sample},
+                      "e2e": {"value": value, "unit": LARGE_UNIT, "h2d_bytes_per_step": 0,
+                              "d2h_bytes_per_step": 0}}), flush=True)
+    return 0
+
+
 def run_reference_datagen(args):
     """The reference's CPU forward (C++ restatement) on a bounded sample of the generation mix."""
     from oracle import native as o
@@ -302,9 +461,15 @@ def main():
     ap.add_argument("--checkpoint", type=int, default=CK)
     ap.add_argument("--nt", type=int, default=NT, help="time steps (profiling runs use a short record)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="gradient", choices=["gradient", "datagen"],
-                    help="gradient: the 256-model misfit-gradient batch (default); datagen: batched generation")
+    ap.add_argument("--workload", default="gradient", choices=["gradient", "datagen", "large"],
+                    help="gradient: the 256-model misfit-gradient batch (default); datagen: batched generation; "
+                         "large: the 800x300 40-shot survey on the streamed path")
+    ap.add_argument("--shots", type=int, default=40, help="shots of the large survey")
     args = ap.parse_args()
+    if args.workload == "large":
+        if args.nt == NT:
+            args.nt = 4000
+        return run_reference_large(args) if args.impl == "reference" else run_large(args)
     if args.workload == "datagen":
         if args.models == MODELS:
             args.models = 4096

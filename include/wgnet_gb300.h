@@ -80,14 +80,18 @@ int wg_evaluate_adjoint_dev(wg_engine* eng, const float* d_vel_mps, const float*
                             double* d_loss, float* d_grad, void* stream);
 
 /* Wavefield checkpoint interval for evaluate_adjoint: snapshots every k steps, segments recomputed
- * in reverse. k <= 0 or k >= nt stores the gradient term of every step (the reference's scheme,
- * wave_wgpu.rs:181-182). No reference counterpart for k > 0. */
+ * in reverse. k >= nt stores the gradient term of every step (the reference's scheme,
+ * wave_wgpu.rs:181-182); so does k <= 0 on the resident path, while on the streamed path k <= 0
+ * (its default) stores every step when that fits in 70% of the free device memory and otherwise
+ * picks the interval that fits. No reference counterpart for k > 0. */
 int wg_set_checkpoint_interval(wg_engine* eng, int k);
 int wg_get_checkpoint_interval(const wg_engine* eng);
 
 /* Named tuning options: "checkpoint_every" (as wg_set_checkpoint_interval), "adjoint_prefetch"
- * (0/1: the column-pair adjoint fetches the next step's stored terms one step ahead). No
- * reference counterpart. */
+ * (0/1: the column-pair adjoint fetches the next step's stored terms one step ahead), "streamed"
+ * (0/1: wavefields in device memory and one launch per time step instead of the resident
+ * kernels; engines whose grid fits no resident kernel start with 1; needs a padded width
+ * nx_vis + 2 (pml + 2) divisible by 4). No reference counterpart. */
 int wg_set_option(wg_engine* eng, const char* key, int value);
 int wg_get_option(const wg_engine* eng, const char* key, int* value);
 

@@ -1,0 +1,117 @@
+"""Parity of the streamed path (wavefields in HBM, one TMA-pipelined launch per time step) with the
+f32 oracle: traces and gradients bit for bit, on small grids forced onto the streamed path, on a
+multi-tile grid, and on the 800 x 300 (5 m) survey that only the streamed path can hold."""
+
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from conftest import layered_model
+from oracle import native as o
+
+pytestmark = pytest.mark.gpu
+
+
+def _engine(sv: o.Survey, streamed: bool | None = True, **kw):
+    from wgnet_gb300.engine import WaveEngine
+
+    eng = WaveEngine(shots=sv.shots, nt=sv.nt, dt=sv.dt, peak_hz=sv.peak_hz, pml=sv.pml, vmin=sv.vmin, vmax=sv.vmax,
+                     nx_vis=sv.nx_vis, nz_vis=sv.nz_vis, h=sv.h, **kw)
+    if streamed is not None:
+        eng.set_option("streamed", int(streamed))
+    return eng
+
+
+def _models(sv, n, seed):
+    v = np.stack([layered_model(seed + i, sv.nz_vis, sv.nx_vis) for i in range(n)])
+    v[0, sv.nz_vis // 3:sv.nz_vis // 2, sv.nx_vis // 4:sv.nx_vis // 2] = 5200.0  # clamped block
+    if n > 1:
+        v[1, 2:5, 3:9] = 800.0
+    return v.astype(np.float32)
+
+
+def test_streamed_small_grid_forward_and_gradient_bitexact(cuda_lib):
+    sv = o.Survey(shots=3, nt=160, dt=0.001, nx_vis=40, nz_vis=36, pml=6)  # padded 56 x 52: one tile wide
+    eng = _engine(sv)
+    assert eng.get_option("streamed") == 1
+    src = eng.sources()
+    vel = _models(sv, 2, 3)
+    ref = o.forward(sv, vel, src, eng.wavelet())
+    np.testing.assert_array_equal(eng.simulate(vel), ref)
+    obs = o.forward(sv, vel * np.float32(1.04), src, eng.wavelet())
+    ref_loss, ref_grad = o.evaluate_adjoint(sv, vel, src, eng.wavelet(), obs)
+    for k in (0, 160, 37, 1):
+        eng.checkpoint_every = k
+        loss, grad = eng.evaluate_adjoint(vel, obs)
+        np.testing.assert_array_equal(grad, ref_grad, err_msg=f"k={k}")
+        np.testing.assert_allclose(loss, ref_loss, rtol=1e-12)
+
+
+def test_streamed_multi_tile_grid_bitexact(cuda_lib):
+    # padded 196 x 134: 4 x 5 tiles, PML strips crossing tile boundaries, receivers over 4 tiles
+    sv = o.Survey(shots=4, nt=220, dt=0.0005, h=5.0, nx_vis=152, nz_vis=90, pml=20)
+    eng = _engine(sv)
+    src = np.array([[0.0, 5.0], [250.0, 5.0], [512.5, 7.5], [755.0, 5.0]], np.float32)
+    eng.set_sources(src)
+    vel = _models(sv, 2, 11)
+    ref = o.forward(sv, vel, src, eng.wavelet())
+    np.testing.assert_array_equal(eng.simulate(vel), ref)
+    obs = o.forward(sv, vel * np.float32(0.96), src, eng.wavelet())
+    ref_loss, ref_grad = o.evaluate_adjoint(sv, vel, src, eng.wavelet(), obs)
+    for k in (0, 50):
+        eng.checkpoint_every = k
+        loss, grad = eng.evaluate_adjoint(vel, obs)
+        np.testing.assert_array_equal(grad, ref_grad, err_msg=f"k={k}")
+        np.testing.assert_allclose(loss, ref_loss, rtol=1e-12)
+
+
+def test_streamed_equals_resident_kernels(cuda_lib):
+    """The same survey through both paths (72 x 72 visible: padded 116, which both can hold)."""
+    sv = o.Survey(shots=5, nt=300, dt=0.001, nx_vis=72, nz_vis=72)
+    vel = _models(sv, 3, 5)
+    res = _engine(sv, streamed=False)
+    if res.get_option("streamed") != 0:
+        pytest.skip("no resident kernel for this grid")
+    st = _engine(sv, streamed=True)
+    np.testing.assert_array_equal(st.simulate(vel), res.simulate(vel))
+    obs = res.simulate(vel * np.float32(1.03))
+    for k in (0, 50):
+        res.checkpoint_every = k
+        st.checkpoint_every = k
+        lr, gr = res.evaluate_adjoint(vel, obs)
+        ls, gs = st.evaluate_adjoint(vel, obs)
+        np.testing.assert_array_equal(gs, gr, err_msg=f"k={k}")
+        np.testing.assert_array_equal(ls, lr)
+
+
+def test_large_survey_800x300_takes_the_streamed_path(cuda_lib):
+    """800 x 300 visible cells at 5 m, dt = 0.5 ms, 40 surface shots, 800 receivers (padded
+    844 x 344), on a shortened record: every gather bit-exact against the oracle, and the gradient
+    of a 2-shot subset."""
+    sv = o.Survey(shots=40, nt=160, dt=0.0005, h=5.0, nx_vis=800, nz_vis=300, pml=20)
+    eng = _engine(sv, streamed=None)
+    assert eng.get_option("streamed") == 1 and (eng.nx, eng.nz) == (844, 344)
+    vel = _models(sv, 1, 2)
+    ref = o.forward(sv, vel, eng.sources(), eng.wavelet())
+    got = eng.simulate(vel)
+    np.testing.assert_array_equal(got, ref)
+    assert np.abs(got).max() > 0
+    sv2 = o.Survey(shots=2, nt=160, dt=0.0005, h=5.0, nx_vis=800, nz_vis=300, pml=20)
+    e2 = _engine(sv2, streamed=None)
+    obs = o.forward(sv2, vel * np.float32(1.02), e2.sources(), e2.wavelet())
+    ref_loss, ref_grad = o.evaluate_adjoint(sv2, vel, e2.sources(), e2.wavelet(), obs)
+    loss, grad = e2.evaluate_adjoint(vel, obs)
+    np.testing.assert_array_equal(grad, ref_grad)
+    np.testing.assert_allclose(loss, ref_loss, rtol=1e-12)
+
+
+def test_streamed_option_errors(cuda_lib):
+    sv = o.Survey(shots=2, nt=20, dt=0.001, nx_vis=70, nz_vis=70)  # padded 114: not divisible by 4
+    eng = _engine(sv, streamed=None)
+    with pytest.raises(Exception):
+        eng.set_option("streamed", 1)
+    assert eng.get_option("streamed") == 0
+    big = _engine(o.Survey(shots=1, nt=20, dt=0.0005, h=5.0, nx_vis=800, nz_vis=300), streamed=None)
+    with pytest.raises(Exception):
+        big.set_option("streamed", 0)

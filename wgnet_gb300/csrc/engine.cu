@@ -145,7 +145,7 @@ struct wg_engine {
   int ck_every = 50;
   int adj_prefetch = 1;
   int streamed = 0;  // 1: wavefields in HBM, one launch per step (grids beyond the resident kernels)
-  wg::StreamWork* sw = nullptr;
+  wg::StreamWork* swork = nullptr;
   // per-kernel timing: (kind, start, stop) events recorded on the launching stream
   bool prof_on = false;
   std::vector<int> prof_kind;
@@ -394,9 +394,17 @@ int create_impl(const wg_config* c, bool cpu_d2, wg_engine** out) {
     rc = set_sources_impl(e, src.data());
   }
   if (rc == WG_OK) rc = set_receivers_impl(e);
-  if (rc == WG_OK && !pick_shapes(e))
-    rc = fail(WG_ERR_UNSUPPORTED, "grid " + std::to_string(e->nx) + "x" + std::to_string(e->nz) +
-                                      " does not fit the resident forward kernel");
+  if (rc == WG_OK && !pick_shapes(e)) {
+    // beyond the resident kernels: the streamed path, with checkpointing sized to the free memory
+    std::string why;
+    if (wg::stream_supported(view_of(e), &why)) {
+      e->streamed = 1;
+      e->ck_every = 0;
+    } else {
+      rc = fail(WG_ERR_UNSUPPORTED, "grid " + std::to_string(e->nx) + "x" + std::to_string(e->nz) +
+                                        " does not fit the resident kernels and " + why);
+    }
+  }
   if (rc != WG_OK) {
     if (e->stream) cudaStreamDestroy(e->stream);
     delete e;
@@ -435,6 +443,33 @@ cudaError_t timed(wg_engine* e, int kind, cudaStream_t st, F&& launch) {
   return cudaEventRecord(b, st);
 }
 
+// Event marks around groups of streamed-path launches (one pair per group, same records as timed()).
+void prof_mark(void* ctx, int kind, bool begin, cudaStream_t st) {
+  auto* e = static_cast<wg_engine*>(ctx);
+  if (!e->prof_on) return;
+  if (begin) {
+    if (e->prof_used + 2 > e->prof_ev.size()) {
+      for (int i = 0; i < 64; ++i) {
+        cudaEvent_t ev;
+        if (cudaEventCreate(&ev) != cudaSuccess) return;
+        e->prof_ev.push_back(ev);
+      }
+    }
+    cudaEventRecord(e->prof_ev[e->prof_used], st);
+  } else if (e->prof_used + 2 <= e->prof_ev.size()) {
+    cudaEventRecord(e->prof_ev[e->prof_used + 1], st);
+    e->prof_used += 2;
+    e->prof_kind.push_back(kind);
+  }
+}
+
+wg::StreamTimer timer_of(wg_engine* e) {
+  wg::StreamTimer t;
+  t.ctx = e;
+  t.fn = prof_mark;
+  return t;
+}
+
 size_t per_model_grad_bytes(const wg_engine* e, int k, bool store_all) {
   const size_t S = e->shots, cells = e->cells;
   size_t b = 2 * cells * 4 + S * e->nt * e->nrec * 4 + 64;
@@ -463,6 +498,10 @@ int chunk_models(const wg_engine* e, int models, size_t per_model) {
 int simulate_dev_impl(wg_engine* e, const float* d_vis, int models, float* d_traces, cudaStream_t st) {
   if (models < 1) return fail(WG_ERR_ARG, "models must be >= 1");
   if (!d_vis || !d_traces) return fail(WG_ERR_ARG, "null pointer");
+  if (e->streamed) {
+    if (!e->swork) e->swork = wg::stream_work_new();
+    return wg::stream_simulate(e->swork, view_of(e), e->rec_cell.data(), d_vis, models, d_traces, st, timer_of(e));
+  }
   const size_t cells = e->cells;
   const int M = chunk_models(e, models, cells * 4 + 64);
   WG_TRY(e->w_vpad.ensure(static_cast<size_t>(M) * cells * 4));
@@ -488,6 +527,11 @@ int gradient_dev_impl(wg_engine* e, const float* d_vis, const float* d_obs, int 
                       cudaStream_t st) {
   if (models < 1) return fail(WG_ERR_ARG, "models must be >= 1");
   if (!d_vis || !d_obs || !d_loss || !d_grad) return fail(WG_ERR_ARG, "null pointer");
+  if (e->streamed) {
+    if (!e->swork) e->swork = wg::stream_work_new();
+    return wg::stream_gradient(e->swork, view_of(e), e->rec_cell.data(), d_vis, d_obs, models, d_loss, d_grad, st,
+                               timer_of(e));
+  }
   if (e->ashape.cluster == 0) return fail(WG_ERR_UNSUPPORTED, "grid does not fit the resident adjoint kernel");
   const bool store_all = e->ck_every <= 0 || e->ck_every >= e->nt;
   const int k = store_all ? e->nt : e->ck_every;
@@ -617,6 +661,7 @@ void wg_engine_destroy(wg_engine* eng) {
     cudaStreamDestroy(eng->stream);
   }
   for (cudaEvent_t ev : eng->prof_ev) cudaEventDestroy(ev);
+  if (eng->swork) wg::stream_work_free(eng->swork);
   delete eng;
 }
 
@@ -767,6 +812,14 @@ int wg_set_option(wg_engine* e, const char* key, int value) {
     e->ck_every = value;
   } else if (k == "adjoint_prefetch") {
     e->adj_prefetch = value ? 1 : 0;
+  } else if (k == "streamed") {
+    if (value) {
+      std::string why;
+      if (!wg::stream_supported(view_of(e), &why)) return fail(WG_ERR_UNSUPPORTED, why);
+    } else if (e->fshape.cluster == 0 || e->ashape.cluster == 0) {
+      return fail(WG_ERR_UNSUPPORTED, "grid does not fit the resident kernels");
+    }
+    e->streamed = value ? 1 : 0;
   } else {
     return fail(WG_ERR_ARG, "unknown option: " + k);
   }
@@ -780,6 +833,8 @@ int wg_get_option(const wg_engine* e, const char* key, int* value) {
     *value = e->ck_every;
   } else if (k == "adjoint_prefetch") {
     *value = e->adj_prefetch;
+  } else if (k == "streamed") {
+    *value = e->streamed;
   } else {
     return fail(WG_ERR_ARG, "unknown option: " + k);
   }
