@@ -148,6 +148,14 @@ void wg_gen_plan_destroy(wg_gen_plan* plan);
  * out != NULL and cap >= n; negative status on bad arguments. */
 int wg_lowpass_taps(double fmax_hz, double dt, float* out, int cap);
 
+/* Tensor-core GEMM used by the learned update network's convolutions (no reference counterpart):
+ * d_d[z][m][n] = sum over k in split z of A[m][k] * B[n][k], A [m][k] and B [n][k] row-major IEEE
+ * bfloat16 (16-byte aligned), FP32 accumulation and output; k a positive multiple of 64, n a
+ * multiple of 4; splits > 1 partitions k and writes one [m][n] partial per split. d_status
+ * receives an error code if a pipeline wait times out. */
+int wg_gemm_bf16_dev(const void* d_a, const void* d_b, float* d_d, int m, int n, int k, int splits, int* d_status,
+                     void* stream);
+
 /* render_residual (python/wgnet/render.py:86-109): activated slot parameters [B][1225][6] ->
  * residual field [B][70][70] in km/s; and its vector-Jacobian product: cotangent [B][70][70] ->
  * parameter gradient [B][1225][6]. Device pointers. */

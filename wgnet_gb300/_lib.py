@@ -65,6 +65,7 @@ SIGNATURES: dict[str, tuple] = {
     "wg_gen_plan_info": (_I, [_P, ctypes.POINTER(_I), ctypes.POINTER(ctypes.c_size_t), _P, _I, ctypes.POINTER(_I)]),
     "wg_gen_plan_destroy": (None, [_P]),
     "wg_lowpass_taps": (_I, [ctypes.c_double, ctypes.c_double, _P, _I]),
+    "wg_gemm_bf16_dev": (_I, [_P, _P, _P, _I, _I, _I, _I, _P, _P]),
     "wg_render_fwd_dev": (_I, [_P, _I, _P, _P]),
     "wg_render_bwd_dev": (_I, [_P, _P, _I, _P, _P]),
     "wg_profile": (_I, [_P, _I]),
