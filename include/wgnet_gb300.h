@@ -156,6 +156,36 @@ int wg_lowpass_taps(double fmax_hz, double dt, float* out, int cap);
 int wg_gemm_bf16_dev(const void* d_a, const void* d_b, float* d_d, int m, int n, int k, int splits, int* d_status,
                      void* stream);
 
+/* Learned update network kernels (no reference counterpart). Activations [B][H][W][C] with
+ * channels contiguous; im2col columns [B H W][Kp] bf16 with k = (3 ky + kx) C + c for the 3x3 taps
+ * at dilation dil (zero outside the grid and for k >= 9 C); weights [N][Kp] bf16 and their
+ * transpose [Kp][N]. All pointers are device pointers; stream NULL = default stream. */
+int wg_pc_im2col(const void* d_act_bf16, int batch, int h, int w, int c, int dil, int kp, void* d_col_bf16,
+                 void* stream);
+/* dact[m][c] (+)= sum over taps of dcol[m'][tap c_count + c] (m' = the pixel whose tap reads m). */
+int wg_pc_col2im(const float* d_dcol, int batch, int h, int w, int c, int dil, int kp, float* d_dact, int accumulate,
+                 void* stream);
+int wg_pc_transpose_bf16(const void* d_in, long rows, int cols, void* d_out, void* stream);
+/* out[r][c] = bf16(relu ? max(x[r][c], 0) : x[r][c]) for the first `cols` of rows of ld floats. */
+int wg_pc_cast_bf16(const float* d_x, long rows, int ld, int cols, int relu, void* d_out, void* stream);
+/* out = a + b (f32) and, if d_out_bf16 != NULL, its bf16 copy. */
+int wg_pc_add(const float* d_a, const float* d_b, long n, float* d_out, void* d_out_bf16, void* stream);
+/* out = d where the bf16 activation mask > 0, else 0. */
+int wg_pc_relu_grad(const float* d_d, const void* d_mask_bf16, long n, float* d_out, void* stream);
+/* Input features [B][h][w][8] bf16: v - 3 (km/s), gradient / its per-sample RMS (written to d_rms),
+ * one-hot band index (4), depth row / h, 0. */
+int wg_pc_features(const float* d_vel_km, const float* d_grad, const int* d_band, int batch, int h, int w,
+                   float* d_rms, void* d_out_bf16, void* stream);
+/* Mean over m of (scale out[m][0] - target[m])^2 added to *d_loss (f64); d_dout[m][0] = its
+ * derivative (other columns untouched). */
+int wg_pc_mse(const float* d_out, int ld, const float* d_target, float scale, long m, double* d_loss, float* d_dout,
+              void* stream);
+/* Adam step on FP32 master weights [n][kp] with the gradient = sum of `splits` partials of its
+ * transpose [splits][kp][n]; writes the bf16 weights and their transpose. d_partial NULL: only
+ * refresh the bf16 copies. */
+int wg_pc_adam(const float* d_partial, int splits, int n, int kp, float* d_w32, float* d_m1, float* d_m2, float lr,
+               float b1, float b2, float eps, int step, void* d_w_bf16, void* d_wt_bf16, void* stream);
+
 /* render_residual (python/wgnet/render.py:86-109): activated slot parameters [B][1225][6] ->
  * residual field [B][70][70] in km/s; and its vector-Jacobian product: cotangent [B][70][70] ->
  * parameter gradient [B][1225][6]. Device pointers. */

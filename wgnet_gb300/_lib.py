@@ -66,6 +66,15 @@ SIGNATURES: dict[str, tuple] = {
     "wg_gen_plan_destroy": (None, [_P]),
     "wg_lowpass_taps": (_I, [ctypes.c_double, ctypes.c_double, _P, _I]),
     "wg_gemm_bf16_dev": (_I, [_P, _P, _P, _I, _I, _I, _I, _P, _P]),
+    "wg_pc_im2col": (_I, [_P, _I, _I, _I, _I, _I, _I, _P, _P]),
+    "wg_pc_col2im": (_I, [_P, _I, _I, _I, _I, _I, _I, _P, _I, _P]),
+    "wg_pc_transpose_bf16": (_I, [_P, ctypes.c_long, _I, _P, _P]),
+    "wg_pc_cast_bf16": (_I, [_P, ctypes.c_long, _I, _I, _I, _P, _P]),
+    "wg_pc_add": (_I, [_P, _P, ctypes.c_long, _P, _P, _P]),
+    "wg_pc_relu_grad": (_I, [_P, _P, ctypes.c_long, _P, _P]),
+    "wg_pc_features": (_I, [_P, _P, _P, _I, _I, _I, _P, _P, _P]),
+    "wg_pc_mse": (_I, [_P, _I, _P, _F, ctypes.c_long, _P, _P, _P]),
+    "wg_pc_adam": (_I, [_P, _I, _I, _I, _P, _P, _P, _F, _F, _F, _F, _I, _P, _P, _P]),
     "wg_render_fwd_dev": (_I, [_P, _I, _P, _P]),
     "wg_render_bwd_dev": (_I, [_P, _P, _I, _P, _P]),
     "wg_profile": (_I, [_P, _I]),
