@@ -156,6 +156,16 @@ int wg_lowpass_taps(double fmax_hz, double dt, float* out, int cap);
 int wg_gemm_bf16_dev(const void* d_a, const void* d_b, float* d_d, int m, int n, int k, int splits, int* d_status,
                      void* stream);
 
+/* FP64 reductions of the batched refinement (python/wgnet/refine.py:41-53): the L-BFGS two-loop
+ * direction dir[b] = -H_b grad[b] from `count[b]` (<= cap) curvature pairs per model stored
+ * oldest first in s/y [models][cap][params], rho [models][cap]; and per-model dot products. One
+ * block per model, fixed reduction order. Device pointers. */
+int wg_lbfgs_direction_dev(const double* d_grad, const double* d_s, const double* d_y, const double* d_rho,
+                           const int* d_count, int models, int cap, long params, double* d_dir, void* stream);
+int wg_dot_f64_dev(const double* d_a, const double* d_b, int models, long params, double* d_out, void* stream);
+/* Per-model misfit 0.5 sum (p - d)^2 / sum d^2 in f64 over per_model values (refine.py:100-104). */
+int wg_misfit_dev(const float* d_pred, const float* d_obs, int models, long per_model, double* d_loss, void* stream);
+
 /* Learned update network kernels (no reference counterpart). Activations [B][H][W][C] with
  * channels contiguous; im2col columns [B H W][Kp] bf16 with k = (3 ky + kx) C + c for the 3x3 taps
  * at dilation dil (zero outside the grid and for k >= 9 C); weights [N][Kp] bf16 and their

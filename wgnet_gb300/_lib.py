@@ -66,6 +66,9 @@ SIGNATURES: dict[str, tuple] = {
     "wg_gen_plan_destroy": (None, [_P]),
     "wg_lowpass_taps": (_I, [ctypes.c_double, ctypes.c_double, _P, _I]),
     "wg_gemm_bf16_dev": (_I, [_P, _P, _P, _I, _I, _I, _I, _P, _P]),
+    "wg_lbfgs_direction_dev": (_I, [_P, _P, _P, _P, _P, _I, _I, ctypes.c_long, _P, _P]),
+    "wg_dot_f64_dev": (_I, [_P, _P, _I, ctypes.c_long, _P, _P]),
+    "wg_misfit_dev": (_I, [_P, _P, _I, ctypes.c_long, _P, _P]),
     "wg_pc_im2col": (_I, [_P, _I, _I, _I, _I, _I, _I, _P, _P]),
     "wg_pc_col2im": (_I, [_P, _I, _I, _I, _I, _I, _I, _P, _I, _P]),
     "wg_pc_transpose_bf16": (_I, [_P, ctypes.c_long, _I, _P, _P]),
