@@ -9,6 +9,7 @@ and the comparison against plain projected L-BFGS.
    refinement (`refine_batch`, dense pixel block + coarse grid, bands 6 / 9 / 12 Hz / full) records
    (field, field gradient, band) at every gradient evaluation; the training target is the
    trajectory's final field minus the recorded field (where plain L-BFGS gets to).
+   With `--target true` (default) the target is the true model minus the recorded field instead.
 2. Training: `UpdateNet.train_step` (tensor-core kernels) on shuffled batches.
 3. Evaluation on held-out seeds with 5-, 3- and 1-shot surveys: plain refinement with the full
    budget, then the learned variant; reported are the wave solves each needs to reach the plain
@@ -54,8 +55,11 @@ def problem(n: int, seed: int, physics: WavePhysics, sigma: float = 5.0):
     return torch.from_numpy(true).cuda(), torch.from_numpy(start).cuda(), obs
 
 
-def trajectories(n_models: int, seed: int, budget: int = 80, chunk: int = 256, nt: int = 1000) -> dict:
-    """Plain refinement trajectories; returns GPU tensors field, grad, band, target and the MAEs."""
+def trajectories(n_models: int, seed: int, budget: int = 80, chunk: int = 256, nt: int = 1000,
+                 target: str = "true") -> dict:
+    """Plain refinement trajectories; returns GPU tensors field, grad, band, target and the MAEs.
+    target "true": the true model minus the recorded field (the training models are synthetic, so
+    the truth is known); "final": the trajectory's final field minus the recorded field."""
     ph = physics_for(SUBSETS[5], nt)
     fields, grads, bands, targets = [], [], [], []
     mae0, mae1 = [], []
@@ -69,7 +73,8 @@ def trajectories(n_models: int, seed: int, budget: int = 80, chunk: int = 256, n
             fields.append(f.cuda())
             grads.append(g.cuda())
             bands.append(b.cuda())
-            targets.append(final[rows] - f.cuda())
+            ref = true[rows] if target == "true" else final[rows]
+            targets.append(ref - f.cuda())
         mae0.append((start - true).abs().mean(dim=(1, 2)))
         mae1.append((final - true).abs().mean(dim=(1, 2)))
     return {"field": torch.cat(fields), "grad": torch.cat(grads), "band": torch.cat(bands).to(torch.int32),
@@ -150,6 +155,7 @@ def main(argv=None) -> int:
     ap.add_argument("--nt", type=int, default=1000)
     ap.add_argument("--out", default="learned_out")
     ap.add_argument("--weights", default=None, help="skip training: load these weights")
+    ap.add_argument("--target", default="true", choices=["true", "final"])
     args = ap.parse_args(argv)
     out = Path(args.out)
     out.mkdir(parents=True, exist_ok=True)
@@ -165,7 +171,7 @@ def main(argv=None) -> int:
         net = UpdateNet.load(args.weights)
     else:
         t0 = time.perf_counter()
-        data = trajectories(args.train_models, seed=1, budget=args.traj_budget, nt=args.nt)
+        data = trajectories(args.train_models, seed=1, budget=args.traj_budget, nt=args.nt, target=args.target)
         torch.cuda.synchronize()
         report["trajectories"] = {"models": args.train_models, "samples": int(data["field"].shape[0]),
                                   "seconds": time.perf_counter() - t0,

@@ -12,9 +12,10 @@ models run in lockstep: every round, the pending evaluations of all models are o
 solve (simulate or evaluate_adjoint over the models that need it); per-model state never mixes.
 
 Learned variant (`proposer=UpdateNet`): at each iteration, before the L-BFGS step, the network
-proposes a dense-block update from (field, field gradient, band); the exact misfit accepts it if
-it lowers the loss (then the gradient there is taken and the curvature pair kept), otherwise the
-iteration falls back to the L-BFGS step and the network is not asked again in that band.
+proposes a dense-block update from (field, field gradient, band), tried at full and then half
+length; the exact misfit accepts it if it lowers the loss (then the gradient there is taken and the
+curvature pair kept), otherwise the iteration falls back to the L-BFGS step and the network is not
+asked again in that band.
 """
 
 from __future__ import annotations
@@ -39,6 +40,7 @@ DENSE_BOUNDS_KM = (1.4, 4.6)
 LBFGS_PAIRS = 8
 LINE_SEARCH_TRIALS = 6
 ARMIJO = 1e-4
+LEARNED_STEPS = (1.0, 0.5)  # lengths at which a learned proposal is tried
 
 
 class RefineResult(NamedTuple):
@@ -310,24 +312,32 @@ def refine_batch(dense_km, observed_full, physics, gaussians=None, budget_solves
                 break
             rows = torch.nonzero(running).flatten()
             accepted = torch.zeros(B, dtype=torch.bool, device=dev)
-            # learned proposal
+            # learned proposal, tried at full length and then at half length
             lp = torch.nonzero(running & learned_ok).flatten()
             if len(lp):
                 f = sp.field(x[lp], lp)
-                upd = proposer.forward(f, cur_gf[lp].float().contiguous(), bidx[lp])
-                cand = x[lp].clone()
-                cand[:, : sp.nd] += upd.reshape(len(lp), -1).double()
-                cand = sp.project(cand)
-                cl = ev.loss(cand, lp, observed)
-                ok = cl < cur_loss[lp]
-                good = lp[ok]
-                if len(good):
-                    gi = torch.nonzero(ok).flatten()
-                    with_grad = good[(solves[good] + 2) <= band_budget[good]]
-                    take(good, cand[gi], cl[gi], with_grad)
-                    accepted[good] = True
-                    log(good, band, cur_loss[good], torch.ones(len(good), dtype=torch.bool), "learned")
-                learned_ok[lp[~ok]] = False
+                upd = proposer.forward(f, cur_gf[lp].float().contiguous(), bidx[lp]).reshape(len(lp), -1).double()
+                trying = torch.ones(len(lp), dtype=torch.bool, device=dev)
+                for scale in LEARNED_STEPS:
+                    trying &= (solves[lp] + 1 < band_budget[lp])
+                    if not bool(trying.any()):
+                        break
+                    ti = torch.nonzero(trying).flatten()
+                    tr = lp[ti]
+                    cand = x[tr].clone()
+                    cand[:, : sp.nd] += scale * upd[ti]
+                    cand = sp.project(cand)
+                    cl = ev.loss(cand, tr, observed)
+                    ok = cl < cur_loss[tr]
+                    if bool(ok.any()):
+                        oi = torch.nonzero(ok).flatten()
+                        good = tr[oi]
+                        with_grad = good[(solves[good] + 2) <= band_budget[good]]
+                        take(good, cand[oi], cl[oi], with_grad)
+                        accepted[good] = True
+                        trying[ti[oi]] = False
+                        log(good, band, cur_loss[good], torch.ones(len(good), dtype=torch.bool), "learned")
+                learned_ok[lp[trying]] = False
             # L-BFGS step for the running models that did not take a learned step
             rows = torch.nonzero(running & ~accepted).flatten()
             if len(rows):
