@@ -39,6 +39,17 @@ struct Cols3 {
   __host__ __device__ static int strip(int x) { return x < SW ? x : x - (NX - 2 * SW); }
 };
 
+// Role of warp `warp` within its segment (0: the PML warp). Warp w issues from scheduler w % 4; with
+// 2 or 4 warps per segment a fixed role per position would put every PML warp (the heavier work) on
+// the same schedulers, so the roles rotate from segment to segment.
+template <int NI>
+__device__ __forceinline__ int warp_role(int warp) {
+  constexpr int W = 1 + NI;
+  const int seg = warp / W, j = warp % W;
+  if constexpr (4 % W == 0) return (j + (seg * W) / 4) % W;
+  return j;
+}
+
 __device__ __forceinline__ float2 lds2(const float* p) { return *reinterpret_cast<const float2*>(p); }
 __device__ __forceinline__ void sts2(float* p, float a, float b) { *reinterpret_cast<float2*>(p) = make_float2(a, b); }
 
@@ -62,7 +73,7 @@ __global__ void __launch_bounds__(NSEG * 32 * (1 + NI), 1) fwd3_kernel(const __g
   const int nz = g.nz, sw = g.sw, region = g.region, nrec = p.st.nrec;
   const float rh = g.rh, dt2 = g.dt2, d2a = g.d2a, d2b = g.d2b;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int seg = warp / (1 + NI), wk = warp % (1 + NI);
+  const int seg = warp / (1 + NI), wk = warp_role<NI>(warp);
   const int rank = (C > 1) ? static_cast<int>(cluster_rank()) : 0;
   const int unit = blockIdx.x / C;
   const int shot = unit % p.st.shots;
@@ -397,7 +408,7 @@ __global__ void __launch_bounds__(NSEG * 32 * (1 + NI), 1) adj3_kernel(const __g
   const int nz = g.nz, swa = g.swa, region = g.region_adj, nrec = p.st.nrec, nt = g.nt;
   const float rh = g.rh, dt2 = g.dt2;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int seg = warp / (1 + NI), wk = warp % (1 + NI);
+  const int seg = warp / (1 + NI), wk = warp_role<NI>(warp);
   const int rank = (C > 1) ? static_cast<int>(cluster_rank()) : 0;
   const int unit = blockIdx.x / C;
   const int shot = unit % p.st.shots;
