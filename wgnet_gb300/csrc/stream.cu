@@ -131,65 +131,88 @@ __device__ __forceinline__ void report(int* status) { atomicCAS(status, 0, ST_CU
 // Forward step t: u_next = v^2 dt^2 w + 2 u - u_prev over every unit, receivers read before the
 // update, source after it (splatForward.wgsl:48-121).
 // ------------------------------------------------------------------------------------------------
+struct FwdMaps {
+  CUtensorMap u;  // wavefield with halo: 72 x 36 boxes over [2 units][nz][nx]
+  CUtensorMap p;  // wavefield without halo (the previous step): 64 x 32 boxes
+  CUtensorMap v;  // velocity: 64 x 32 boxes over [models][nz][nx]
+};
+constexpr int FST = 3;                                        // forward pipeline stages
+constexpr int FSTAGE_F = BZ * BX + 2 * TZ_ * TX_;             // floats per stage: U | P | V
+constexpr size_t kFwdSmem = FST * FSTAGE_F * 4 + 128 + 8 * FST;
+
+// Issue the three copies of job `job` into stage buffer `st` with barrier `bar`.
+__device__ __forceinline__ void issue_fwd(const SArgs& a, const FwdMaps& m, float* st, uint64_t* bar, int job,
+                                          int par) {
+  const int tiles = a.tiles_x * a.tiles_z;
+  const int unit = job / tiles, tile = job % tiles;
+  const int tz = tile / a.tiles_x, tx = tile % a.tiles_x;
+  mbar_expect_tx(bar, FSTAGE_F * 4);
+  tma_load(st, &m.u, tx * TX_ - HX, tz * TZ_ - HZ, par * a.units + unit, bar);
+  tma_load(st + BZ * BX, &m.p, tx * TX_, tz * TZ_, (1 - par) * a.units + unit, bar);
+  tma_load(st + BZ * BX + TZ_ * TX_, &m.v, tx * TX_, tz * TZ_, unit / a.shots, bar);
+}
+
 template <bool TRACES, bool STORE>
-__global__ void __launch_bounds__(NTH, 3) fwd_stream_kernel(const __grid_constant__ CUtensorMap map,
-                                                         const __grid_constant__ SArgs a) {
-  __shared__ __align__(128) float stage[2 * BZ * BX];
-  __shared__ __align__(8) uint64_t bar[2];
+__global__ void __launch_bounds__(NTH, 2) fwd_stream_kernel(const __grid_constant__ FwdMaps maps,
+                                                            const __grid_constant__ SArgs a) {
+  extern __shared__ __align__(128) float fsm_raw[];
+  float* stage = fsm_raw + ((128 - (smem_u32(fsm_raw) & 127)) & 127) / 4;  // [FST][U | P | V]
+  uint64_t* bar = reinterpret_cast<uint64_t*>(stage + FST * FSTAGE_F);
   const int tid = threadIdx.x;
   const int tiles = a.tiles_x * a.tiles_z;
   const int jobs = a.units * tiles;
   const int par = a.t & 1;
   const int nx = a.nx, nz = a.nz, ssw = a.ssw, region = a.region;
   const size_t cells = static_cast<size_t>(nx) * nz;
-  Pipe pipe{bar, stage};
   if (tid == 0) {
-    mbar_init(&bar[0], 1);
-    mbar_init(&bar[1], 1);
+    for (int k = 0; k < FST; ++k) mbar_init(&bar[k], 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   __syncthreads();
   int job = blockIdx.x;
-  if (tid == 0 && job < jobs) issue(a, &map, pipe, job, 0, par);
+  if (tid == 0)
+    for (int k = 0; k < FST - 1; ++k)
+      if (job + k * static_cast<int>(gridDim.x) < jobs)
+        issue_fwd(a, maps, stage + k * FSTAGE_F, &bar[k], job + k * gridDim.x, par);
   const float f = __ldg(&a.wavelet[a.t]);
   const int pc = tid & 31, grp = tid >> 5;
   for (int i = 0; job < jobs; ++i, job += gridDim.x) {
-    const int s = i & 1;
-    const int nxt = job + gridDim.x;
-    if (tid == 0 && nxt < jobs) {
+    const int s = i % FST;
+    const int ahead = job + (FST - 1) * gridDim.x;
+    if (tid == 0 && ahead < jobs) {
+      // the stage refilled here was last read in iteration i - 1, which every thread has left
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-      issue(a, &map, pipe, nxt, s ^ 1, par);
+      const int sa = (i + FST - 1) % FST;
+      issue_fwd(a, maps, stage + sa * FSTAGE_F, &bar[sa], ahead, par);
+    }
+    // a wait that runs out (the copy never completed) ends the kernel in every thread together,
+    // after thread 0 has waited, again bounded, for the copies it issued for the next tiles
+    if (__syncthreads_or(mbar_wait(&bar[s], (i / FST) & 1) ? 0 : 1)) {
+      if (tid == 0) {
+        report(a.status);
+        for (int k = 1; k < FST; ++k)
+          if (job + k * static_cast<int>(gridDim.x) < jobs) mbar_wait(&bar[(i + k) % FST], ((i + k) / FST) & 1);
+      }
+      return;
     }
     const int unit = job / tiles, tile = job % tiles;
     const int tzi = tile / a.tiles_x, txi = tile % a.tiles_x;
     const int x0 = txi * TX_, z0 = tzi * TZ_;
-    const int model = unit / a.shots, shot = unit % a.shots;
+    const int shot = unit % a.shots;
     const int x = x0 + 2 * pc;
     const int zr = z0 + RPT * grp;
     const bool xok = x >= FD_PAD && x + 1 < nx - FD_PAD;
     const bool xpml = x < region || x + 1 >= nx - region;
     float* Wn = a.W + (static_cast<size_t>(1 - par) * a.units + unit) * cells;
-    const float* vel = a.vel + static_cast<size_t>(model) * cells;
-    // own-cell inputs (previous wavefield, velocity), requested before the tile copy is waited for
+    const float* Pt = stage + s * FSTAGE_F + BZ * BX;
+    const float* Vt = Pt + TZ_ * TX_;
     float2 pv[RPT], vv[RPT];
 #pragma unroll
     for (int r = 0; r < RPT; ++r) {
-      const int z = zr + r;
-      const bool ok = xok && z >= FD_PAD && z < nz - FD_PAD;
-      const int cell = (ok ? z : FD_PAD) * nx + (ok ? x : FD_PAD);
-      pv[r] = ld2(Wn + cell);
-      vv[r] = ldg2(vel + cell);
+      pv[r] = lds2(Pt + (RPT * grp + r) * TX_ + 2 * pc);
+      vv[r] = lds2(Vt + (RPT * grp + r) * TX_ + 2 * pc);
     }
-    // a wait that runs out (the copy never completed) ends the kernel in every thread together,
-    // after thread 0 has waited, again bounded, for the copy it issued for the next tile
-    if (__syncthreads_or(mbar_wait(&bar[s], (i >> 1) & 1) ? 0 : 1)) {
-      if (tid == 0) {
-        report(a.status);
-        if (nxt < jobs) mbar_wait(&bar[s ^ 1], ((i + 1) >> 1) & 1);
-      }
-      return;
-    }
-    const float* T = stage + s * BZ * BX;
+    const float* T = stage + s * FSTAGE_F;
 
     if (TRACES) {
       const int r0 = a.tile_rec_start[tile], r1 = a.tile_rec_start[tile + 1];
@@ -616,18 +639,27 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
 }
 
 // Tensor map over [2 * units][nz][nx] floats with a 72 x 36 x 1 box; out-of-range elements read 0.
-int make_map(CUtensorMap* m, float* base, int nx, int nz, int units) {
+int make_map(CUtensorMap* m, const float* base, int nx, int nz, int depth, int box_x = BX, int box_z = BZ) {
   auto fn = encode_fn();
   if (!fn) return report_error(WG_ERR_CUDA, "cuTensorMapEncodeTiled is not available");
   const cuuint64_t dims[3] = {static_cast<cuuint64_t>(nx), static_cast<cuuint64_t>(nz),
-                              static_cast<cuuint64_t>(2) * units};
+                              static_cast<cuuint64_t>(depth)};
   const cuuint64_t strides[2] = {static_cast<cuuint64_t>(nx) * 4, static_cast<cuuint64_t>(nx) * nz * 4};
-  const cuuint32_t box[3] = {BX, BZ, 1};
+  const cuuint32_t box[3] = {static_cast<cuuint32_t>(box_x), static_cast<cuuint32_t>(box_z), 1};
   const cuuint32_t es[3] = {1, 1, 1};
-  CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, base, dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+  CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float*>(base), dims, strides, box, es,
+                  CU_TENSOR_MAP_INTERLEAVE_NONE,
                   CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS) return report_error(WG_ERR_CUDA, ("cuTensorMapEncodeTiled failed: " + std::to_string(r)).c_str());
   return WG_OK;
+}
+
+// Forward maps: the wavefield pair with and without halo, and the models' velocity.
+int make_fwd_maps(FwdMaps* m, const float* W, const float* vel, int nx, int nz, int units, int models) {
+  int rc = make_map(&m->u, W, nx, nz, 2 * units);
+  if (rc == WG_OK) rc = make_map(&m->p, W, nx, nz, 2 * units, TX_, TZ_);
+  if (rc == WG_OK) rc = make_map(&m->v, vel, nx, nz, models, TX_, TZ_);
+  return rc;
 }
 
 constexpr size_t kAdjSmem = (7 * BZ * BX) * 4 + 16 + 128;
@@ -698,7 +730,13 @@ int occupancy(StreamWork* w) {
   SW_CK(cudaGetDevice(&dev));
   SW_CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
   SW_CK(cudaFuncSetAttribute(adj_stream_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(kAdjSmem)));
-  SW_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fb, fwd_stream_kernel<true, true>, NTH, 0));
+  SW_CK(cudaFuncSetAttribute(fwd_stream_kernel<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             static_cast<int>(kFwdSmem)));
+  SW_CK(cudaFuncSetAttribute(fwd_stream_kernel<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             static_cast<int>(kFwdSmem)));
+  SW_CK(cudaFuncSetAttribute(fwd_stream_kernel<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             static_cast<int>(kFwdSmem)));
+  SW_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fb, fwd_stream_kernel<true, true>, NTH, kFwdSmem));
   SW_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ab, adj_stream_kernel, NTH, kAdjSmem));
   w->sms = sms;
   w->fwd_blocks = sms * std::max(fb, 1);
@@ -752,17 +790,17 @@ int alloc_forward(StreamWork* w, const EngineView& v, int units, cudaStream_t st
 }
 
 // One forward step over all units.
-int fwd_step(StreamWork* w, const CUtensorMap& map, SArgs a, int t, bool traces, bool store, cudaStream_t st) {
+int fwd_step(StreamWork* w, const FwdMaps& map, SArgs a, int t, bool traces, bool store, cudaStream_t st) {
   a.t = t;
   const int jobs = a.units * a.tiles_x * a.tiles_z;
   const int blocks = std::min(jobs, w->fwd_blocks);
   note_launch();
   if (traces && store)
-    fwd_stream_kernel<true, true><<<blocks, NTH, 0, st>>>(map, a);
+    fwd_stream_kernel<true, true><<<blocks, NTH, kFwdSmem, st>>>(map, a);
   else if (traces)
-    fwd_stream_kernel<true, false><<<blocks, NTH, 0, st>>>(map, a);
+    fwd_stream_kernel<true, false><<<blocks, NTH, kFwdSmem, st>>>(map, a);
   else
-    fwd_stream_kernel<false, true><<<blocks, NTH, 0, st>>>(map, a);
+    fwd_stream_kernel<false, true><<<blocks, NTH, kFwdSmem, st>>>(map, a);
   SW_CK(cudaGetLastError());
   return WG_OK;
 }
@@ -828,8 +866,8 @@ int stream_simulate(StreamWork* w, const EngineView& v, const int* h_rec_cell, c
   note_launch();
   SW_CK(launch_pad_velocity(d_vis, models, v.nx_vis, v.nz_vis, v.pad, v.vmin, v.vmax, w->vpad.f(), nullptr, st));
   if ((rc = alloc_forward(w, v, units, st)) != WG_OK) return rc;
-  CUtensorMap map;
-  if ((rc = make_map(&map, w->W.f(), v.nx, v.nz, units)) != WG_OK) return rc;
+  FwdMaps map;
+  if ((rc = make_fwd_maps(&map, w->W.f(), w->vpad.f(), v.nx, v.nz, units, models)) != WG_OK) return rc;
   SArgs a = base_args(w, v, units);
   a.vel = w->vpad.f();
   a.W = w->W.f();
@@ -903,8 +941,8 @@ int stream_gradient(StreamWork* w, const EngineView& v, const int* h_rec_cell, c
   SW_CK(w->stored.ensure(static_cast<size_t>(seg) * step_bytes));
   if (J > 1) SW_CK(w->ckpt.ensure(static_cast<size_t>(J - 1) * slot_bytes));
 
-  CUtensorMap fmap;
-  if ((rc = make_map(&fmap, w->W.f(), v.nx, v.nz, units)) != WG_OK) return rc;
+  FwdMaps fmap;
+  if ((rc = make_fwd_maps(&fmap, w->W.f(), w->vpad.f(), v.nx, v.nz, units, models)) != WG_OK) return rc;
   SArgs f = base_args(w, v, units);
   f.vel = w->vpad.f();
   f.W = w->W.f();
@@ -940,7 +978,7 @@ int stream_gradient(StreamWork* w, const EngineView& v, const int* h_rec_cell, c
   SW_CK(cudaMemsetAsync(w->LZZ.p, 0, 2 * units * zsf * 4, st));
   SW_CK(cudaMemsetAsync(w->gacc.p, 0, units * cells * 4, st));
   CUtensorMap amap;
-  if ((rc = make_map(&amap, w->L.f(), v.nx, v.nz, units)) != WG_OK) return rc;
+  if ((rc = make_map(&amap, w->L.f(), v.nx, v.nz, 2 * units)) != WG_OK) return rc;
   SArgs b = base_args(w, v, units);
   b.vel = w->vpad.f();
   b.W = w->L.f();
