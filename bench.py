@@ -2,7 +2,8 @@
 
 Workload (one "step"): the misfit gradient of a batch of 256 mixed-family 70 x 70 velocity models
 (10 m cells, pml 20 -> 114 x 114 padded), 5 surface shots at cells 0/17/34/52/69, 70 receivers,
-15 Hz Ricker, dt = 1 ms, nt = 1000, wavefield checkpoints every 50 steps with recomputation.
+15 Hz Ricker, dt = 1 ms, nt = 1000, wavefield checkpoints every 100 steps with recomputation
+(k = 25 and 50 with --checkpoint).
 Observed data come from the true models; the gradient is taken at their 5-cell Gaussian-smoothed
 versions. Data are synthetic (seeded), in the shapes and value ranges of the reference's setting.
 
@@ -39,7 +40,7 @@ NT = 1000
 DT = 0.001
 NX = 70
 PML = 20
-CK = 50
+CK = 100
 UPDATED_CELLS = (NX + 2 * (PML + 2) - 4) ** 2  # 110 x 110 cells updated per step
 FLOPS_PER_CELL_UPDATE = 48.0  # average over interior / one-PML-axis / two-PML-axes cells at pml 20
 # DRAM bytes per (unit, step) measured with ncu on the small case (32 models, nt 200) and scaled by
@@ -461,6 +462,7 @@ def main():
     ap.add_argument("--checkpoint", type=int, default=CK)
     ap.add_argument("--nt", type=int, default=NT, help="time steps (profiling runs use a short record)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true", help="keep the engine's default launch shapes")
     ap.add_argument("--workload", default="gradient", choices=["gradient", "datagen", "large"],
                     help="gradient: the 256-model misfit-gradient batch (default); datagen: batched generation; "
                          "large: the 800x300 40-shot survey on the streamed path")
@@ -501,6 +503,11 @@ def main():
     eng = WaveEngine(shots=SHOTS, nt=nt, dt=DT, peak_hz=15.0, pml=PML, vmin=1000.0, vmax=5000.0,
                      checkpoint_every=args.checkpoint)
     eng.set_sources(src)
+    tuned = None
+    if not args.no_autotune:
+        from wgnet_gb300.autotune import tune
+
+        tuned = tune(eng)  # launch shapes timed per kernel (cached per GPU and survey)
     dev = torch.device("cuda", local)
     d_true = torch.from_numpy(true).to(dev)
     d_obs = eng.simulate_torch(d_true)
@@ -601,7 +608,8 @@ def main():
                                f"pml 20, checkpoint every {args.checkpoint} steps", "models_per_step": M,
                    "shots": SHOTS, "nt": nt, "checkpoint_every": args.checkpoint,
                    "l2": "inputs larger than L2 (observed 358 MB, checkpoints ~10 GB per step)",
-                   "launch_shape": {"forward": eng.launch_shape("forward"), "adjoint": eng.launch_shape("adjoint")}},
+                   "launch_shape": {"forward": eng.launch_shape("forward"), "adjoint": eng.launch_shape("adjoint")},
+                   "autotuned": tuned is not None},
         "gcell_updates_per_s": cells_per_s / 1e9,
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": launches,

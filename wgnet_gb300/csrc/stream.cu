@@ -138,7 +138,7 @@ struct FwdMaps {
 };
 constexpr int FST = 3;                                        // forward pipeline stages
 constexpr int FSTAGE_F = BZ * BX + 2 * TZ_ * TX_;             // floats per stage: U | P | V
-constexpr size_t kFwdSmem = FST * FSTAGE_F * 4 + 128 + 8 * FST;
+constexpr size_t kFwdSmem = FST * FSTAGE_F * 4 + 128 + 16 * FST;
 
 // Issue the three copies of job `job` into stage buffer `st` with barrier `bar`.
 __device__ __forceinline__ void issue_fwd(const SArgs& a, const FwdMaps& m, float* st, uint64_t* bar, int job,
@@ -152,12 +152,24 @@ __device__ __forceinline__ void issue_fwd(const SArgs& a, const FwdMaps& m, floa
   tma_load(st + BZ * BX + TZ_ * TX_, &m.v, tx * TX_, tz * TZ_, unit / a.shots, bar);
 }
 
+constexpr int FWD_THREADS = NTH + 32;  // 8 consumer warps + 1 producer warp
+
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+// Warp-specialised: warp 8 (one lane) streams the jobs' tiles into FST stages (waiting on each
+// stage's "empty" barrier before refilling it), warps 0-7 update the tiles and release each stage
+// with one arrival per warp. No CTA-wide barrier per tile: consumer warps run up to FST tiles
+// apart. Every wait is bounded; a consumer that gives up records the error and leaves; the
+// producer that gives up records it and waits (bounded) for the copies it issued.
 template <bool TRACES, bool STORE>
-__global__ void __launch_bounds__(NTH, 2) fwd_stream_kernel(const __grid_constant__ FwdMaps maps,
-                                                            const __grid_constant__ SArgs a) {
+__global__ void __launch_bounds__(FWD_THREADS, 2) fwd_stream_kernel(const __grid_constant__ FwdMaps maps,
+                                                                    const __grid_constant__ SArgs a) {
   extern __shared__ __align__(128) float fsm_raw[];
   float* stage = fsm_raw + ((128 - (smem_u32(fsm_raw) & 127)) & 127) / 4;  // [FST][U | P | V]
-  uint64_t* bar = reinterpret_cast<uint64_t*>(stage + FST * FSTAGE_F);
+  uint64_t* full = reinterpret_cast<uint64_t*>(stage + FST * FSTAGE_F);
+  uint64_t* empty = full + FST;
   const int tid = threadIdx.x;
   const int tiles = a.tiles_x * a.tiles_z;
   const int jobs = a.units * tiles;
@@ -165,34 +177,37 @@ __global__ void __launch_bounds__(NTH, 2) fwd_stream_kernel(const __grid_constan
   const int nx = a.nx, nz = a.nz, ssw = a.ssw, region = a.region;
   const size_t cells = static_cast<size_t>(nx) * nz;
   if (tid == 0) {
-    for (int k = 0; k < FST; ++k) mbar_init(&bar[k], 1);
+    for (int k = 0; k < FST; ++k) {
+      mbar_init(&full[k], 1);
+      mbar_init(&empty[k], NTH / 32);
+    }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   __syncthreads();
-  int job = blockIdx.x;
-  if (tid == 0)
-    for (int k = 0; k < FST - 1; ++k)
-      if (job + k * static_cast<int>(gridDim.x) < jobs)
-        issue_fwd(a, maps, stage + k * FSTAGE_F, &bar[k], job + k * gridDim.x, par);
+  if (tid >= NTH) {  // producer warp
+    if (tid == NTH) {
+      int issued = 0;
+      for (int job = blockIdx.x; job < jobs; job += gridDim.x, ++issued) {
+        const int s = issued % FST;
+        if (issued >= FST && !mbar_wait(&empty[s], (issued / FST - 1) & 1)) {
+          report(a.status);
+          for (int k = 1; k <= FST && issued - k >= 0; ++k)  // the copies still landing
+            mbar_wait(&full[(issued - k) % FST], ((issued - k) / FST) & 1);
+          return;
+        }
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        issue_fwd(a, maps, stage + s * FSTAGE_F, &full[s], job, par);
+      }
+    }
+    return;
+  }
   const float f = __ldg(&a.wavelet[a.t]);
   const int pc = tid & 31, grp = tid >> 5;
+  int job = blockIdx.x;
   for (int i = 0; job < jobs; ++i, job += gridDim.x) {
     const int s = i % FST;
-    const int ahead = job + (FST - 1) * gridDim.x;
-    if (tid == 0 && ahead < jobs) {
-      // the stage refilled here was last read in iteration i - 1, which every thread has left
-      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-      const int sa = (i + FST - 1) % FST;
-      issue_fwd(a, maps, stage + sa * FSTAGE_F, &bar[sa], ahead, par);
-    }
-    // a wait that runs out (the copy never completed) ends the kernel in every thread together,
-    // after thread 0 has waited, again bounded, for the copies it issued for the next tiles
-    if (__syncthreads_or(mbar_wait(&bar[s], (i / FST) & 1) ? 0 : 1)) {
-      if (tid == 0) {
-        report(a.status);
-        for (int k = 1; k < FST; ++k)
-          if (job + k * static_cast<int>(gridDim.x) < jobs) mbar_wait(&bar[(i + k) % FST], ((i + k) / FST) & 1);
-      }
+    if (!mbar_wait(&full[s], (i / FST) & 1)) {
+      report(a.status);
       return;
     }
     const int unit = job / tiles, tile = job % tiles;
@@ -341,7 +356,8 @@ __global__ void __launch_bounds__(NTH, 2) fwd_stream_kernel(const __grid_constan
       }
       st2(Wn + cell, n0, n1);
     }
-    __syncthreads();  // every read of this stage is done before it is refilled
+    __syncwarp();
+    if (pc == 0) mbar_arrive(&empty[s]);  // this warp is done with the stage
   }
 }
 
@@ -736,7 +752,7 @@ int occupancy(StreamWork* w) {
                              static_cast<int>(kFwdSmem)));
   SW_CK(cudaFuncSetAttribute(fwd_stream_kernel<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              static_cast<int>(kFwdSmem)));
-  SW_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fb, fwd_stream_kernel<true, true>, NTH, kFwdSmem));
+  SW_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fb, fwd_stream_kernel<true, true>, FWD_THREADS, kFwdSmem));
   SW_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ab, adj_stream_kernel, NTH, kAdjSmem));
   w->sms = sms;
   w->fwd_blocks = sms * std::max(fb, 1);
@@ -796,11 +812,11 @@ int fwd_step(StreamWork* w, const FwdMaps& map, SArgs a, int t, bool traces, boo
   const int blocks = std::min(jobs, w->fwd_blocks);
   note_launch();
   if (traces && store)
-    fwd_stream_kernel<true, true><<<blocks, NTH, kFwdSmem, st>>>(map, a);
+    fwd_stream_kernel<true, true><<<blocks, FWD_THREADS, kFwdSmem, st>>>(map, a);
   else if (traces)
-    fwd_stream_kernel<true, false><<<blocks, NTH, kFwdSmem, st>>>(map, a);
+    fwd_stream_kernel<true, false><<<blocks, FWD_THREADS, kFwdSmem, st>>>(map, a);
   else
-    fwd_stream_kernel<false, true><<<blocks, NTH, kFwdSmem, st>>>(map, a);
+    fwd_stream_kernel<false, true><<<blocks, FWD_THREADS, kFwdSmem, st>>>(map, a);
   SW_CK(cudaGetLastError());
   return WG_OK;
 }
