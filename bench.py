@@ -423,6 +423,88 @@ def run_reference_large(args):
     return 0
 
 
+def run_train(args):
+    """Learned update network: training throughput (samples/s) of `UpdateNet.train_step` on batches
+    of 32 synthetic 70x70 samples, and the tensor-core GEMM of one 64 -> 64 3x3 convolution layer
+    (M = 32 x 4900 pixels, N = 64, K = 576) timed alone against the measured bf16 peak."""
+    import ctypes
+
+    import torch
+
+    from wgnet_gb300 import _lib
+    from wgnet_gb300.models_synth import make_batch, smooth
+    from wgnet_gb300.precond import UpdateNet
+
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    B = 32
+    v = make_batch(B, seed=3) / 1000.0
+    s0 = smooth(v, 5.0)
+    vel = torch.from_numpy(s0.astype(np.float32)).cuda()
+    grad = torch.randn((B, 70, 70), device="cuda") * 0.01
+    band = torch.tensor([i % 4 for i in range(B)], dtype=torch.int32, device="cuda")
+    target = torch.from_numpy((v - s0).astype(np.float32)).cuda()
+    net = UpdateNet(seed=0)
+    for _ in range(args.warmup):
+        net.train_step(vel, grad, band, target, lr=1e-4)
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    _lib.launch_count(reset=True)
+    ev0.record()
+    for _ in range(args.steps):
+        net.train_step(vel, grad, band, target, lr=1e-4)
+    ev1.record()
+    torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1) / args.steps
+    launches = _lib.launch_count() // max(args.steps, 1)
+    # one convolution GEMM alone
+    lib = _lib.load()
+    M, N, K = B * 4900, 64, 576
+    a = torch.randn((M, K), device="cuda").to(torch.bfloat16)
+    b = torch.randn((N, K), device="cuda").to(torch.bfloat16)
+    d = torch.empty((M, N), device="cuda")
+    st = torch.zeros(4, dtype=torch.int32, device="cuda")
+
+    def gemm():
+        _lib.check(lib.wg_gemm_bf16_dev(ctypes.c_void_p(a.data_ptr()), ctypes.c_void_p(b.data_ptr()),
+                                        ctypes.c_void_p(d.data_ptr()), M, N, K, 1, ctypes.c_void_p(st.data_ptr()),
+                                        ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)))
+
+    for _ in range(5):
+        gemm()
+    torch.cuda.synchronize()
+    reps = 50
+    ev0.record()
+    for _ in range(reps):
+        gemm()
+    ev1.record()
+    torch.cuda.synchronize()
+    gms = ev0.elapsed_time(ev1) / reps
+    tflops = 2.0 * M * N * K / (gms / 1000.0) / 1e12
+    # with N = 64 output channels the GEMM reads its im2col operand once: 52 flops per byte, below
+    # the ridge point, so the HBM roofline bounds it (algorithmic bytes: A, B read, D written)
+    gemm_bytes = M * K * 2 + N * K * 2 + M * N * 4
+    hbm_peak, peak_kind = measured_peaks()
+    bf16_peak = None
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        bf16_peak = float(json.loads(p.read_text()).get("bf16_tflops", 0.0)) or None
+    line = {"metric": "update-network training samples/s (70x70, batch 32)", "value": B / (ms / 1000.0),
+            "unit": "samples/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "bf16 weights, f32 accumulate",
+            "data": "synthetic", "config": {"workload": "UpdateNet.train_step, batch 32, 447,552 parameters",
+                                           "batch": B},
+            "gpu_launches": launches,
+            "roofline": {"kernel": "gemm_bf16_kernel (conv 64->64, M 156800, N 64, K 576)", "bound": "hbm",
+                         "achieved": gemm_bytes / (gms / 1000.0) / 1e9, "peak": hbm_peak, "unit": "GB/s",
+                         "frac": gemm_bytes / (gms / 1000.0) / 1e9 / hbm_peak, "peak_source": peak_kind,
+                         "traffic": None, "bytes_per_launch": gemm_bytes, "avg_launch_ms": gms},
+            "tensor": {"achieved_tflops": tflops, "bf16_peak_tflops": bf16_peak,
+                       "frac": (tflops / bf16_peak) if bf16_peak else None,
+                       "flops_per_byte": 2.0 * M * N * K / gemm_bytes}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def run_reference_datagen(args):
     """The reference's CPU forward (C++ restatement) on a bounded sample of the generation mix."""
     from oracle import native as o
@@ -463,11 +545,13 @@ def main():
     ap.add_argument("--nt", type=int, default=NT, help="time steps (profiling runs use a short record)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-autotune", action="store_true", help="keep the engine's default launch shapes")
-    ap.add_argument("--workload", default="gradient", choices=["gradient", "datagen", "large"],
+    ap.add_argument("--workload", default="gradient", choices=["gradient", "datagen", "large", "train"],
                     help="gradient: the 256-model misfit-gradient batch (default); datagen: batched generation; "
                          "large: the 800x300 40-shot survey on the streamed path")
     ap.add_argument("--shots", type=int, default=40, help="shots of the large survey")
     args = ap.parse_args()
+    if args.workload == "train":
+        return run_train(args)
     if args.workload == "large":
         if args.nt == NT:
             args.nt = 4000

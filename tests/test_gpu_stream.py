@@ -7,7 +7,7 @@ from __future__ import annotations
 import numpy as np
 import pytest
 
-from conftest import layered_model
+from conftest import layered_model, rel_l2
 from oracle import native as o
 
 pytestmark = pytest.mark.gpu
@@ -97,6 +97,10 @@ def test_large_survey_800x300_takes_the_streamed_path(cuda_lib):
     got = eng.simulate(vel)
     np.testing.assert_array_equal(got, ref)
     assert np.abs(got).max() > 0
+    ref64 = o.forward(sv, vel, eng.sources(), eng.wavelet(), precision="f64")
+    err64 = rel_l2(got, ref64)
+    print(f"800x300 gathers: rel L2 vs FP32 oracle 0, vs FP64 oracle {err64:.2e}")
+    assert err64 < 1e-5
     sv2 = o.Survey(shots=2, nt=160, dt=0.0005, h=5.0, nx_vis=800, nz_vis=300, pml=20)
     e2 = _engine(sv2, streamed=None)
     obs = o.forward(sv2, vel * np.float32(1.02), e2.sources(), e2.wavelet())
@@ -104,6 +108,10 @@ def test_large_survey_800x300_takes_the_streamed_path(cuda_lib):
     loss, grad = e2.evaluate_adjoint(vel, obs)
     np.testing.assert_array_equal(grad, ref_grad)
     np.testing.assert_allclose(loss, ref_loss, rtol=1e-12)
+    _, g64 = o.evaluate_adjoint(sv2, vel, e2.sources(), e2.wavelet(), obs, precision="f64")
+    gerr = rel_l2(grad, g64)
+    print(f"800x300 gradient: rel L2 vs FP32 oracle 0, vs FP64 oracle {gerr:.2e}")
+    assert gerr < 1e-4
 
 
 def test_streamed_option_errors(cuda_lib):
