@@ -6,9 +6,10 @@
 // transposed columns x transposed output gradient, split along the reduction).
 //
 // One CTA computes a 128 x 64 tile of D with 128 threads. Thread 0 is the producer and the MMA
-// issuer: it keeps STAGES k-tiles (64 wide) in flight with TMA (2-D boxes of 8 elements x rows,
-// which land in shared memory as the canonical no-swizzle K-major layout of 8-row x 16-byte core
-// matrices), waits for a stage's mbarrier, issues four tcgen05.mma (M 128, N 64, K 16) into the
+// issuer: it keeps STAGES k-tiles (64 wide) in flight with TMA (one 2-D box of 64 elements = 128
+// bytes x rows per operand, written with the 128-byte swizzle, the K-major SWIZZLE_128B layout of
+// the tensor cores: 8-row x 128-byte atoms), waits for a stage's mbarrier, issues four tcgen05.mma
+// (M 128, N 64, K 16; each K slice starts 32 bytes further into the swizzled rows) into the
 // TMEM accumulator and commits them to the stage's "empty" mbarrier, which frees the stage for the
 // next copy. After the last k-tile the four warps read the accumulator back with tcgen05.ld (warp w
 // owns TMEM lanes 32w..32w+31 = rows of the tile) and store it. Every wait is bounded: on time-out
@@ -63,15 +64,17 @@ __device__ __forceinline__ void tma2d(void* dst, const CUtensorMap* map, int x, 
       : "memory");
 }
 
-// Shared-memory matrix descriptor, no swizzle, K-major: core matrices of 8 rows x 16 bytes, rows
-// 16 bytes apart; lbo = bytes between core matrices along K, sbo = along M/N.
-__device__ __forceinline__ uint64_t sdesc(const void* p, unsigned lbo, unsigned sbo) {
+// Shared-memory matrix descriptor, K-major with the 128-byte swizzle: rows of 128 bytes, atoms of
+// 8 rows (sbo = 1024 bytes between atoms along M/N; lbo unused for this layout, encoded as 1). The
+// tile base is 1024-byte aligned, so the base-offset field stays 0.
+__device__ __forceinline__ uint64_t sdesc_sw128(const void* p) {
   uint64_t d = 0;
   d |= static_cast<uint64_t>((su32(p) >> 4) & 0x3FFF);
-  d |= static_cast<uint64_t>((lbo >> 4) & 0x3FFF) << 16;
-  d |= static_cast<uint64_t>((sbo >> 4) & 0x3FFF) << 32;
-  d |= static_cast<uint64_t>(1) << 46;  // descriptor version for the 5th-generation tensor cores
-  return d;                             // base offset 0, swizzle mode 0 (none)
+  d |= static_cast<uint64_t>(1) << 16;              // leading byte offset (unused), 16 bytes
+  d |= static_cast<uint64_t>(1024 >> 4) << 32;      // stride byte offset: 8 rows x 128 bytes
+  d |= static_cast<uint64_t>(1) << 46;              // descriptor version for the 5th-generation tensor cores
+  d |= static_cast<uint64_t>(2) << 61;              // layout: 128-byte swizzle
+  return d;
 }
 
 // Instruction descriptor of kind::f16: BF16 A and B, FP32 D, both K-major, M x N.
@@ -109,8 +112,8 @@ __global__ void __launch_bounds__(NTHR, 1) gemm_bf16_kernel(const __grid_constan
                                                             const __grid_constant__ GemmArgs g) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char* smem = smem_raw + ((1024 - (su32(smem_raw) & 1023)) & 1023);
-  unsigned char* sA = smem;                              // [STAGES][BK/8][BM][16 B]
-  unsigned char* sB = smem + STAGES * kStageA;           // [STAGES][BK/8][BN][16 B]
+  unsigned char* sA = smem;                              // [STAGES][BM][128 B], swizzled
+  unsigned char* sB = smem + STAGES * kStageA;           // [STAGES][BN][128 B], swizzled
   uint64_t* full = reinterpret_cast<uint64_t*>(sB + STAGES * kStageB);
   uint64_t* empty = full + STAGES;
   uint64_t* done = empty + STAGES;
@@ -146,11 +149,8 @@ __global__ void __launch_bounds__(NTHR, 1) gemm_bf16_kernel(const __grid_constan
     auto load = [&](int kt, int s) {
       bar_expect(&full[s], kStageA + kStageB);
       const int kx = (kt0 + kt) * BK;
-#pragma unroll
-      for (int c = 0; c < BK / 8; ++c) {
-        tma2d(sA + s * kStageA + c * BM * 16, &mapA, kx + 8 * c, m0, &full[s]);
-        tma2d(sB + s * kStageB + c * BN * 16, &mapB, kx + 8 * c, n0, &full[s]);
-      }
+      tma2d(sA + s * kStageA, &mapA, kx, m0, &full[s]);
+      tma2d(sB + s * kStageB, &mapB, kx, n0, &full[s]);
       ++issued[s];
     };
     const int pre = KT < STAGES ? KT : STAGES;
@@ -167,9 +167,9 @@ __global__ void __launch_bounds__(NTHR, 1) gemm_bf16_kernel(const __grid_constan
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 #pragma unroll
       for (int kk = 0; kk < BK / 16; ++kk) {
-        // K = 16 covers two 8-element core-matrix columns: 2 * (rows * 16) bytes further along K
-        const uint64_t a = sdesc(sA + s * kStageA + kk * 2 * BM * 16, BM * 16, 128);
-        const uint64_t b = sdesc(sB + s * kStageB + kk * 2 * BN * 16, BN * 16, 128);
+        // K slice kk: 16 elements = 32 bytes further into every (swizzled) 128-byte row
+        const uint64_t a = sdesc_sw128(sA + s * kStageA + kk * 32);
+        const uint64_t b = sdesc_sw128(sB + s * kStageB + kk * 32);
         mma_bf16(tmem, a, b, idesc, (kt > 0 || kk > 0) ? 1u : 0u);
       }
       mma_commit(&empty[s]);
@@ -202,9 +202,12 @@ __global__ void __launch_bounds__(NTHR, 1) gemm_bf16_kernel(const __grid_constan
     atomicCAS(g.status, 0, ST_CUDA);
   }
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-  // epilogue: warp w reads TMEM lanes 32w..32w+31 (tile rows), 64 columns
-  const int row = m0 + warp * 32 + (tid & 31);
-  float* drow = g.D + static_cast<size_t>(blockIdx.z) * g.M * g.ldd + static_cast<size_t>(row) * g.ldd + n0;
+  // epilogue: warp w reads TMEM lanes 32w..32w+31 (tile rows), 64 columns, into a [BM][BN + 4]
+  // staging tile in shared memory (the pipeline buffers, idle now), then the warps write whole rows
+  // of the tile (coalesced 256-byte rows)
+  float* stile = reinterpret_cast<float*>(smem);
+  constexpr int LD = BN + 4;
+  const int lrow = warp * 32 + (tid & 31);
 #pragma unroll
   for (int c0 = 0; c0 < BN; c0 += 16) {
     uint32_t r[16];
@@ -216,19 +219,27 @@ __global__ void __launch_bounds__(NTHR, 1) gemm_bf16_kernel(const __grid_constan
           "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
         : "r"(taddr));
     asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-    if (row < g.M) {
 #pragma unroll
-      for (int j = 0; j < 16; j += 4) {
-        if (n0 + c0 + j + 3 < g.N) {
-          const float4 v = have ? make_float4(__uint_as_float(r[j]), __uint_as_float(r[j + 1]),
-                                              __uint_as_float(r[j + 2]), __uint_as_float(r[j + 3]))
-                                : make_float4(0.f, 0.f, 0.f, 0.f);
-          *reinterpret_cast<float4*>(drow + c0 + j) = v;
-        } else {
-          for (int q = 0; q < 4; ++q)
-            if (n0 + c0 + j + q < g.N) drow[c0 + j + q] = have ? __uint_as_float(r[j + q]) : 0.f;
-        }
-      }
+    for (int j = 0; j < 16; j += 4)
+      *reinterpret_cast<float4*>(stile + lrow * LD + c0 + j) =
+          have ? make_float4(__uint_as_float(r[j]), __uint_as_float(r[j + 1]), __uint_as_float(r[j + 2]),
+                             __uint_as_float(r[j + 3]))
+               : make_float4(0.f, 0.f, 0.f, 0.f);
+  }
+  __syncthreads();
+  float* dtile = g.D + static_cast<size_t>(blockIdx.z) * g.M * g.ldd + static_cast<size_t>(m0) * g.ldd + n0;
+  const int ncols = min(BN, g.N - n0);
+  for (int e = tid; e < BM * (BN / 4); e += NTHR) {
+    const int rr = e / (BN / 4), c4 = (e % (BN / 4)) * 4;
+    if (m0 + rr >= g.M) continue;
+    const float4 v = *reinterpret_cast<const float4*>(stile + rr * LD + c4);
+    float* dst = dtile + static_cast<size_t>(rr) * g.ldd + c4;
+    if (c4 + 3 < ncols) {
+      *reinterpret_cast<float4*>(dst) = v;
+    } else {
+      const float vv[4] = {v.x, v.y, v.z, v.w};
+      for (int q = 0; q < 4; ++q)
+        if (c4 + q < ncols) dst[q] = vv[q];
     }
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -248,16 +259,17 @@ PFN_cuTensorMapEncodeTiled_v12000 encode() {
   return fn;
 }
 
-// 2-D map over a row-major [rows][K] bf16 matrix, boxes of 8 elements x box_rows.
+// 2-D map over a row-major [rows][K] bf16 matrix, boxes of 64 elements (128 bytes) x box_rows,
+// written to shared memory with the 128-byte swizzle.
 int map_bf16(CUtensorMap* m, const void* base, long rows, long K, int box_rows) {
   auto fn = encode();
   if (!fn) return report_error(WG_ERR_CUDA, "cuTensorMapEncodeTiled is not available");
   const cuuint64_t dims[2] = {static_cast<cuuint64_t>(K), static_cast<cuuint64_t>(rows)};
   const cuuint64_t strides[1] = {static_cast<cuuint64_t>(K) * 2};
-  const cuuint32_t box[2] = {8, static_cast<cuuint32_t>(box_rows)};
+  const cuuint32_t box[2] = {BK, static_cast<cuuint32_t>(box_rows)};
   const cuuint32_t es[2] = {1, 1};
   CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides, box, es,
-                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS) return report_error(WG_ERR_CUDA, ("cuTensorMapEncodeTiled(bf16) failed: " + std::to_string(r)).c_str());
   return WG_OK;
