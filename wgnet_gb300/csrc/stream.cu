@@ -127,6 +127,21 @@ __device__ __forceinline__ void issue(const SArgs& a, const CUtensorMap* map, Pi
 
 __device__ __forceinline__ void report(int* status) { atomicCAS(status, 0, ST_CUDA); }
 
+// A tile (with its halo) clear of the PML strips, the grid frame, the receivers' rows and this
+// unit's source corners: every pair of every row takes the interior formulas.
+__device__ __forceinline__ bool interior_tile(const SArgs& a, int x0, int z0, const int* sc) {
+  const int m = a.ssw;
+  if (x0 - HX < m || x0 + TX_ + HX > a.nx - m || z0 - HZ < m || z0 + TZ_ + HZ > a.nz - m) return false;
+  if (z0 + TZ_ > a.rec_z0 && z0 <= a.rec_z1) return false;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const int c = __ldg(&sc[k]);
+    const int cz = c / a.nx, cx = c % a.nx;
+    if (cz >= z0 && cz < z0 + TZ_ && cx >= x0 && cx < x0 + TX_) return false;
+  }
+  return true;
+}
+
 // ------------------------------------------------------------------------------------------------
 // Forward step t: u_next = v^2 dt^2 w + 2 u - u_prev over every unit, receivers read before the
 // update, source after it (splatForward.wgsl:48-121).
@@ -228,6 +243,39 @@ __global__ void __launch_bounds__(FWD_THREADS, 2) fwd_stream_kernel(const __grid
       vv[r] = lds2(Vt + (RPT * grp + r) * TX_ + 2 * pc);
     }
     const float* T = stage + s * FSTAGE_F;
+
+    if (interior_tile(a, x0, z0, a.st.src_cell + 4 * shot)) {
+      // interior tile: no frame, PML, receivers or sources
+      const int sx = 2 * pc + HX, sz = RPT * grp + HZ;
+      float2 col[RPT + 4];
+#pragma unroll
+      for (int k = 0; k < RPT + 4; ++k) col[k] = lds2(T + (sz - 2 + k) * BX + sx);
+      float* stp = STORE ? a.stored + (static_cast<size_t>(unit) * a.seg + (a.t - a.seg_t0)) * cells : nullptr;
+#pragma unroll
+      for (int r = 0; r < RPT; ++r) {
+        const int cell = (zr + r) * nx + x;
+        const float2 A = lds2(T + (sz + r) * BX + sx - 2);
+        const float2 B = lds2(T + (sz + r) * BX + sx + 2);
+        const float u0 = col[r + 2].x, u1 = col[r + 2].y;
+        const float2 zm2 = col[r], zm1 = col[r + 1], zp1 = col[r + 3], zp2 = col[r + 4];
+        const float d2x0 = (((F_D2A * u0 + F_D2B * (u1 + A.y)) - F_D2C * (B.x + A.x)) * a.d2a) * a.d2b;
+        const float d2x1 = (((F_D2A * u1 + F_D2B * (B.x + u0)) - F_D2C * (B.y + A.y)) * a.d2a) * a.d2b;
+        const float d2z0 = (((F_D2A * u0 + F_D2B * (zp1.x + zm1.x)) - F_D2C * (zp2.x + zm2.x)) * a.d2a) * a.d2b;
+        const float d2z1 = (((F_D2A * u1 + F_D2B * (zp1.y + zm1.y)) - F_D2C * (zp2.y + zm2.y)) * a.d2a) * a.d2b;
+        const float w0 = d2x0 + d2z0, w1 = d2x1 + d2z1;
+        const float2 v = vv[r];
+        const float v20 = (v.x * v.x) * a.dt2, v21 = (v.y * v.y) * a.dt2;
+        const float n0 = ((v20 * w0) + (2.0f * u0)) - pv[r].x;
+        const float n1 = ((v21 * w1) + (2.0f * u1)) - pv[r].y;
+        if (STORE)
+          __stcs(reinterpret_cast<float2*>(stp + cell),
+                 make_float2(((2.0f * v.x) * a.dt2) * w0, ((2.0f * v.y) * a.dt2) * w1));
+        st2(Wn + cell, n0, n1);
+      }
+      __syncwarp();
+      if (pc == 0) mbar_arrive(&empty[s]);
+      continue;
+    }
 
     if (TRACES) {
       const int r0 = a.tile_rec_start[tile], r1 = a.tile_rec_start[tile + 1];
@@ -460,6 +508,43 @@ __global__ void __launch_bounds__(NTH) adj_stream_kernel(const __grid_constant__
       return;
     }
     const float* L = stage + s * BZ * BX;
+
+    if (interior_tile(a, x0, z0, a.st.src_cell + 4 * shot)) {
+      // interior tile: VS over the tile and halo, then the interior update
+#pragma unroll
+      for (int d = 0; d < DER; ++d) {
+        const int e = tid + d * NTH;
+        if (e >= BZ * (BX / 2)) break;
+        const int o = (e / (BX / 2)) * BX + 2 * (e % (BX / 2));
+        const float2 l = lds2(L + o);
+        st2(VS + o, ((vd[d].x * vd[d].x) * a.dt2) * l.x, ((vd[d].y * vd[d].y) * a.dt2) * l.y);
+      }
+      __syncthreads();
+      const int sx = 2 * pc + HX, sz = RPT * grp + HZ;
+      float* Lnf = a.W + (static_cast<size_t>(1 - q) * a.units + unit) * cells;
+      float* gf = a.gacc + static_cast<size_t>(unit) * cells;
+#pragma unroll
+      for (int r = 0; r < RPT; ++r) {
+        const int cell = (zr + r) * nx + x;
+        const int so = (sz + r) * BX + sx;
+        const float2 Vb = lds2(VS + so), Va = lds2(VS + so - 2), Vc = lds2(VS + so + 2);
+        const float2 Vm2 = lds2(VS + so - 2 * BX), Vm1 = lds2(VS + so - BX), Vp1 = lds2(VS + so + BX),
+                     Vp2 = lds2(VS + so + 2 * BX);
+        float w0 = ((((F_D2A * Vb.x) + (F_D2B * (Vb.y + Va.y))) + (A_D2C * (Vc.x + Va.x))) * a.rh) * a.rh;
+        float w1 = ((((F_D2A * Vb.y) + (F_D2B * (Vc.x + Vb.x))) + (A_D2C * (Vc.y + Va.y))) * a.rh) * a.rh;
+        w0 = w0 + ((((F_D2A * Vb.x) + (F_D2B * (Vp1.x + Vm1.x))) + (A_D2C * (Vp2.x + Vm2.x))) * a.rh) * a.rh;
+        w1 = w1 + ((((F_D2A * Vb.y) + (F_D2B * (Vp1.y + Vm1.y))) + (A_D2C * (Vp2.y + Vm2.y))) * a.rh) * a.rh;
+        const float2 lc = lds2(L + so);
+        const float n0 = (w0 + (2.0f * lc.x)) - lpv[r].x;
+        const float n1 = (w1 + (2.0f * lc.y)) - lpv[r].y;
+        const float g0 = 0.0f + ((lc.x * stv[r].x) * 1.0f);
+        const float g1 = 0.0f + ((lc.y * stv[r].y) * 1.0f);
+        st2(gf + cell, gav[r].x + g0, gav[r].y + g1);
+        st2(Lnf + cell, n0, n1);
+      }
+      __syncthreads();  // stage and VS are reused by the next tile
+      continue;
+    }
 
     // derived terms over the tile and its halo (pairs of columns x0-4+2j, rows z0-2+k)
 #pragma unroll
