@@ -103,6 +103,17 @@ def make_physics(physics) -> None:
     np.savez_compressed(HERE / "physics.npz", **out)
 
 
+def make_metrics(render) -> None:
+    """field_metrics (render.py:140-152) on seeded smooth random fields."""
+    gen = torch.Generator().manual_seed(5)
+    target = 1.5 + 3.0 * torch.rand(4, 70, 70, generator=gen)
+    target = torch.nn.functional.avg_pool2d(target[:, None], 5, stride=1, padding=2)[:, 0]
+    pred = target + 0.1 * torch.randn(4, 70, 70, generator=gen)
+    m = render.field_metrics(pred, target)
+    np.savez(HERE / "metrics.npz", pred=pred.numpy(), target=target.numpy(),
+             **{k: v.numpy() for k, v in m.items()})
+
+
 def make_refine(refine) -> None:
     rng = np.random.default_rng(11)
     out = {}
@@ -127,6 +138,7 @@ def main() -> None:
     make_render(mods["render"])
     make_physics(mods["physics"])
     make_refine(mods["refine"])
+    make_metrics(mods["render"])
     for p in sorted(HERE.glob("*.npz")):
         print(p.name, p.stat().st_size)
 

@@ -210,3 +210,15 @@ def test_layered_model_generator():
     v = layered_model(0)
     assert v.shape == (70, 70) and v.min() >= 1500 and v.max() <= 4500
     assert (np.diff(v[:, 0]) >= 0).all()
+
+
+def test_field_metrics_match_reference_golden():
+    """field_metrics / ssim (python/wgnet/render.py:116-152) against the reference's own output."""
+    import torch
+
+    from wgnet_gb300.render import field_metrics
+
+    m = np.load(GOLD / "metrics.npz")
+    got = field_metrics(torch.from_numpy(m["pred"]), torch.from_numpy(m["target"]))
+    for k in ("mae_mps", "rmse_mps", "ssim", "mae_norm", "mse_norm"):
+        np.testing.assert_allclose(got[k].numpy(), m[k], rtol=1e-6, atol=0, err_msg=k)
