@@ -288,12 +288,14 @@ int gemm_bf16(const void* A, const void* B, float* D, int M, int N, int K, int s
   int rc = map_bf16(&ma, A, M, K, BM);
   if (rc != WG_OK) return rc;
   if ((rc = map_bf16(&mb, B, N, K, BN)) != WG_OK) return rc;
-  static bool attr = false;
-  if (!attr) {
+  static bool attr[64] = {};  // the shared-memory attribute is set once per device
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return report_error(WG_ERR_CUDA, "no device");
+  if (!attr[dev]) {
     cudaError_t e = cudaFuncSetAttribute(gemm_bf16_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          static_cast<int>(kGemmSmem));
     if (e != cudaSuccess) return report_error(WG_ERR_CUDA, cudaGetErrorString(e));
-    attr = true;
+    attr[dev] = true;
   }
   const int KT = K / BK;
   const int per = (KT + splits - 1) / splits;
