@@ -568,22 +568,18 @@ def main():
 
     import torch
 
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    torch.cuda.set_device(local)
-    dist = None
-    if world > 1:
-        import torch.distributed as dist
+    from wgnet_gb300 import replicas
 
-        dist.init_process_group("nccl")
+    rank, world, local = replicas.env()
+    torch.cuda.set_device(local)
+    dist = replicas.init("nccl")
 
     from wgnet_gb300 import _lib
     from wgnet_gb300.engine import WaveEngine
 
     lib = _lib.load()
     M = args.models
-    true, start, src = workload(M, seed=rank)
+    true, start, src = workload(M, seed=replicas.rank_seed(0, rank))
     eng = WaveEngine(shots=SHOTS, nt=nt, dt=DT, peak_hz=15.0, pml=PML, vmin=1000.0, vmax=5000.0,
                      checkpoint_every=args.checkpoint)
     eng.set_sources(src)
@@ -611,8 +607,7 @@ def main():
     th = threading.Thread(target=clocks_sampler, args=(stop, clk), daemon=True)
     th.start()
     time.sleep(0.3)
-    if dist:
-        dist.barrier()
+    replicas.barrier(dist)
     torch.cuda.synchronize()
     lib.wg_profile(eng._h, 1)
     _lib.launch_count(reset=True)
@@ -630,11 +625,9 @@ def main():
     lib.wg_profile(eng._h, 0)
     stop.set()
     th.join(timeout=2)
-    if dist:
-        t = torch.tensor([ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    value = world * M * args.steps / (ms / 1000.0)
+    replicas.barrier(dist)
+    ms = replicas.max_over_ranks(ms, dist, dev)
+    value = replicas.aggregate_rate(M, args.steps, world, ms)
     ms_step = ms / args.steps
     assert torch.isfinite(loss).all() and torch.isfinite(grad).all()
 
@@ -649,17 +642,14 @@ def main():
                                            h_grad.data_ptr()))
 
     host_step()
-    if dist:
-        dist.barrier()
+    replicas.barrier(dist)
     t0 = time.perf_counter()
     for _ in range(args.steps):
         host_step()
     e2e_s = time.perf_counter() - t0
-    if dist:
-        t = torch.tensor([e2e_s], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
-    e2e = world * M * args.steps / e2e_s
+    replicas.barrier(dist)
+    e2e_s = replicas.max_over_ranks(e2e_s, dist, dev)
+    e2e = replicas.aggregate_rate(M, args.steps, world, e2e_s * 1000.0)
     h2d = h_vel.numel() * 4 + h_obs.numel() * 4
     d2h = h_loss.numel() * 8 + h_grad.numel() * 4
 
