@@ -230,7 +230,7 @@ def run_datagen(args):
         "metric": DATAGEN_METRIC, "value": value, "unit": DATAGEN_UNIT, "n_gpus": 1, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32 (FP16 output)", "data": "synthetic (seeded mixed-family models)",
-        "config": {"workload": f"config 2 batched generation: {total} models round-robin over 70x70/100x100/140x140, "
+        "config": {"workload": f"batched generation: {total} models round-robin over 70x70/100x100/140x140, "
                                f"5 shots, nt={args.nt}, dt=1ms, low-pass + x4 decimation to FP16, one CUDA graph launch",
                    "counts": counts, "l2": "inputs and outputs larger than L2 (f32 traces ~8 GB per step)",
                    "kernels_per_graph": gen.kernels_per_launch},
@@ -362,7 +362,7 @@ def run_large(args):
         "metric": LARGE_METRIC, "value": value, "unit": LARGE_UNIT, "n_gpus": 1, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded faulted layered model, smoothed start)",
-        "config": {"workload": f"config 4 large survey: 800x300 cells at 5 m (padded 844x344), {shots} shots, "
+        "config": {"workload": f"large survey: 800x300 cells at 5 m (padded 844x344), {shots} shots, "
                                f"800 receivers, dt=0.5ms, nt={nt}, forward + exact adjoint gradient, streamed path",
                    "checkpointing": "every step's gradient term stored in HBM when it fits (auto)",
                    "l2": "inputs larger than L2 (wavefields ~93 MB + stored terms ~186 GB per gradient)"},
@@ -678,7 +678,7 @@ def main():
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded mixed-family models: flat, curved, faulted, blob inclusions)",
-        "config": {"workload": f"config 3 gradient batch: {M} mixed-family 70x70 models x 5 shots, nt={nt}, dt=1ms, "
+        "config": {"workload": f"gradient batch: {M} mixed-family 70x70 models x 5 shots, nt={nt}, dt=1ms, "
                                f"pml 20, checkpoint every {args.checkpoint} steps", "models_per_step": M,
                    "shots": SHOTS, "nt": nt, "checkpoint_every": args.checkpoint,
                    "l2": "inputs larger than L2 (observed 358 MB, checkpoints ~10 GB per step)",

@@ -1,4 +1,4 @@
-"""Config-3 checks of the gradient path on the GPU: the adjoint dot-product test
+"""Checks of the gradient path on the GPU: the adjoint dot-product test
 <J dv, r> = <dv, J^T r> (J from central differences of the FP64 oracle forward, J^T from the CUDA
 adjoint), and gradients flowing through the Gaussian renderer to offset / scale / angle /
 amplitude (WaveLoss + render_residual autograd against FP64 finite differences of the oracle)."""

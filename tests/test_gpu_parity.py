@@ -40,7 +40,7 @@ def make_engine(sv: o.Survey, src, **kw):
     return eng
 
 
-def config1():
+def survey_70x70():
     """70x70, dt = 1 ms, nt = 1000, sources at cells 0, 17, 34, 52, 69, every surface receiver."""
     sv = o.Survey(shots=5, nt=1000, dt=0.001)
     src = np.stack([np.float32([0, 17, 34, 52, 69]) * np.float32(10.0), np.full(5, 10.0, np.float32)], 1)
@@ -59,8 +59,8 @@ def test_forward_bitexact_small(cuda_lib):
         np.testing.assert_array_equal(got, ref, err_msg=f"shape {shape}")
 
 
-def test_forward_bitexact_config1(cuda_lib):
-    sv, src = config1()
+def test_forward_bitexact_70x70_nt1000(cuda_lib):
+    sv, src = survey_70x70()
     eng = make_engine(sv, src)
     vel = np.stack([layered_model(0), layered_model(1)])
     got = eng.simulate(vel)
@@ -70,7 +70,7 @@ def test_forward_bitexact_config1(cuda_lib):
     err_gpu, err_cpu = rel_l2(got[:1], ref64), rel_l2(ref[:1], ref64)
     assert rel_l2(got, ref) <= GATHER_TOL
     assert err_gpu <= err_cpu * 1.0000001 + 1e-12
-    print(f"\n[config1 forward] rel L2 vs FP32 oracle {rel_l2(got, ref):.3e}, vs FP64 oracle {err_gpu:.3e}")
+    print(f"\n[70x70 nt 1000 forward] rel L2 vs FP32 oracle {rel_l2(got, ref):.3e}, vs FP64 oracle {err_gpu:.3e}")
 
 
 def test_simulate_shot_cpu_dropin_bitexact(cuda_lib):
@@ -112,8 +112,8 @@ def test_adjoint_all_shapes_agree(cuda_lib):
         np.testing.assert_array_equal(grad, rg, err_msg=f"shape {shape}")
 
 
-def test_adjoint_config1_parity(cuda_lib):
-    sv, src = config1()
+def test_adjoint_parity_70x70_nt1000(cuda_lib):
+    sv, src = survey_70x70()
     eng = make_engine(sv, src, checkpoint_every=50)
     wav = eng.wavelet()
     true = layered_model(3)
@@ -125,7 +125,7 @@ def test_adjoint_config1_parity(cuda_lib):
     np.testing.assert_array_equal(grad, rg)
     np.testing.assert_allclose(loss, rl, rtol=1e-12)
     l64, g64 = o.evaluate_adjoint(sv, cur, src, wav, obs, precision="f64")
-    print(f"\n[config1 gradient] rel L2 vs FP32 oracle {rel_l2(grad, rg):.3e}, vs FP64 oracle {rel_l2(grad, g64):.3e}; "
+    print(f"\n[70x70 nt 1000 gradient] rel L2 vs FP32 oracle {rel_l2(grad, rg):.3e}, vs FP64 oracle {rel_l2(grad, g64):.3e}; "
           f"loss {loss[0]:.6e} (FP64 {l64[0]:.6e})")
 
 
@@ -166,7 +166,7 @@ def test_reference_fd_check_on_gpu(cuda_lib):
 
 
 def test_gpu_gradient_vs_fp64_finite_differences(cuda_lib):
-    """Config-3 style check: FD with eps = 1e-3 m/s on the FP64 oracle vs the GPU adjoint."""
+    """FD with eps = 1e-3 m/s on the FP64 oracle vs the GPU adjoint."""
     sv, vel, src = small_case(seed=7, nt=200)
     vel = np.clip(vel, 1500, 4500).astype(np.float32)
     eng = make_engine(sv, src, checkpoint_every=25)
