@@ -573,10 +573,23 @@ int gradient_dev_impl(wg_engine* e, const float* d_vis, const float* d_obs, int 
       f.stored = e->w_stored.as<float>();
       WG_LAUNCH(timed(e, K_FWD, st, [&] { return wg::launch_fwd(e->fshape, true, true, f, st); }));
     } else {
-      f.ck_out = slots > 0 ? e->w_ckpt.as<float>() : nullptr;
+      // Steps [0, (J-1) k] with receivers and checkpoints (the last checkpoint is written at the
+      // start of step (J-1) k, which is computed once more below), then the last segment from
+      // that checkpoint with receivers and stored terms: the reverse sweep starts without a
+      // recompute.
+      f.ck_out = e->w_ckpt.as<float>();
       f.ck_every = k;
       f.ck_slots = slots;
+      f.t1 = (J - 1) * k + 1;
       WG_LAUNCH(timed(e, K_FWD, st, [&] { return wg::launch_fwd(e->fshape, true, false, f, st); }));
+      wg::FwdArgs l = f;
+      l.t0 = (J - 1) * k;
+      l.t1 = e->nt;
+      l.ck_out = nullptr;
+      l.ck_in = e->w_ckpt.as<float>();
+      l.ck_in_slot = J - 2;
+      l.stored = e->w_stored.as<float>();
+      WG_LAUNCH(timed(e, K_FWD, st, [&] { return wg::launch_fwd(e->fshape, true, true, l, st); }));
     }
     WG_LAUNCH(wg::launch_residual(e->w_traces.as<float>(), obs, e->w_scale.as<float>(), mc, S * tr,
                                   e->w_traces.as<float>(), d_loss + m0, st));
@@ -613,7 +626,8 @@ int gradient_dev_impl(wg_engine* e, const float* d_vis, const float* d_obs, int 
         r.ck_every = k;
         r.stored = e->w_stored.as<float>();
         r.status = e->d_status.as<int>();
-        WG_LAUNCH(timed(e, K_RECOMPUTE, st, [&] { return wg::launch_fwd(e->fshape, false, true, r, st); }));
+        if (j < J - 1)  // the last segment's terms are already stored by the first pass
+          WG_LAUNCH(timed(e, K_RECOMPUTE, st, [&] { return wg::launch_fwd(e->fshape, false, true, r, st); }));
         a.t_hi = t1;
         a.t_lo = t0;
         a.first = (j == J - 1) ? 1 : 0;

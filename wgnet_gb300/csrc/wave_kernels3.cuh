@@ -642,8 +642,10 @@ __global__ void __launch_bounds__(NSEG * 32 * (1 + NI), 1) adj3_kernel(const __g
         float n0 = (w0 + (2.0f * lc[i][0])) - lp[i][0];
         float n1 = (w1 + (2.0f * lc[i][1])) - lp[i][1];
         const float2 sv = PREF ? stv[PREF ? i : 0] : __ldcs(reinterpret_cast<const float2*>(st_t + i * NX));
-        float g0 = 0.0f + ((lc[i][0] * sv.x) * 1.0f);
-        float g1 = 0.0f + ((lc[i][1] * sv.y) * 1.0f);
+        // the shader starts the per-step gradient at +0; starting from the product itself differs
+        // only in the sign of an exact zero
+        float g0 = (lc[i][0] * sv.x) * 1.0f;
+        float g1 = (lc[i][1] * sv.y) * 1.0f;
         if (recmask & (3u << (2 * i))) {
           const int cell = gbase + i * NX;
           const int e1 = p.st.csr[cell + 1], e2 = p.st.csr[cell + 2];
