@@ -145,6 +145,8 @@ struct wg_engine {
   int ck_every = 50;
   int adj_prefetch = 1;
   int streamed = 0;  // 1: wavefields in HBM, one launch per step (grids beyond the resident kernels)
+  cudaStream_t copy_stream = nullptr;  // host->device copy of observed data, overlapping the forward
+  cudaEvent_t obs_ready = nullptr;
   wg::StreamWork* swork = nullptr;
   // per-kernel timing: (kind, start, stop) events recorded on the launching stream
   bool prof_on = false;
@@ -523,8 +525,10 @@ int simulate_dev_impl(wg_engine* e, const float* d_vis, int models, float* d_tra
   return WG_OK;
 }
 
+// obs_ready (optional): an event the observed data's arrival is recorded on; nothing reads them
+// before the first forward pass has been launched, so their host->device copy can overlap it.
 int gradient_dev_impl(wg_engine* e, const float* d_vis, const float* d_obs, int models, double* d_loss, float* d_grad,
-                      cudaStream_t st) {
+                      cudaStream_t st, cudaEvent_t obs_ready = nullptr) {
   if (models < 1) return fail(WG_ERR_ARG, "models must be >= 1");
   if (!d_vis || !d_obs || !d_loss || !d_grad) return fail(WG_ERR_ARG, "null pointer");
   if (e->streamed) {
@@ -558,8 +562,6 @@ int gradient_dev_impl(wg_engine* e, const float* d_vis, const float* d_obs, int 
     WG_LAUNCH(wg::launch_pad_velocity(d_vis + static_cast<size_t>(m0) * e->nx_vis * e->nz_vis, mc, e->nx_vis,
                                       e->nz_vis, e->pad, e->cfg.vmin, e->cfg.vmax, e->w_vpad.as<float>(),
                                       e->w_mask.as<float>(), st));
-    WG_LAUNCH(wg::launch_energy(obs, mc, S * tr, e->w_energy.as<double>(), e->w_scale.as<float>(),
-                                e->d_status.as<int>(), st));
     wg::FwdArgs f{};
     f.g = e->grid();
     f.st = e->stations();
@@ -591,6 +593,9 @@ int gradient_dev_impl(wg_engine* e, const float* d_vis, const float* d_obs, int 
       l.stored = e->w_stored.as<float>();
       WG_LAUNCH(timed(e, K_FWD, st, [&] { return wg::launch_fwd(e->fshape, true, true, l, st); }));
     }
+    if (obs_ready && m0 == 0) WG_CK(cudaStreamWaitEvent(st, obs_ready, 0));
+    WG_LAUNCH(wg::launch_energy(obs, mc, S * tr, e->w_energy.as<double>(), e->w_scale.as<float>(),
+                                e->d_status.as<int>(), st));
     WG_LAUNCH(wg::launch_residual(e->w_traces.as<float>(), obs, e->w_scale.as<float>(), mc, S * tr,
                                   e->w_traces.as<float>(), d_loss + m0, st));
     WG_CK(cudaMemsetAsync(e->w_gacc.p, 0, static_cast<size_t>(units) * cells * 4, st));
@@ -675,6 +680,11 @@ void wg_engine_destroy(wg_engine* eng) {
     cudaStreamDestroy(eng->stream);
   }
   for (cudaEvent_t ev : eng->prof_ev) cudaEventDestroy(ev);
+  if (eng->obs_ready) cudaEventDestroy(eng->obs_ready);
+  if (eng->copy_stream) {
+    cudaStreamSynchronize(eng->copy_stream);
+    cudaStreamDestroy(eng->copy_stream);
+  }
   if (eng->swork) wg::stream_work_free(eng->swork);
   delete eng;
 }
@@ -800,9 +810,23 @@ int wg_evaluate_adjoint(wg_engine* e, const float* vel, const float* obs, int mo
   WG_TRY(e->w_grad.ensure(nv * 4));
   WG_CK(cudaMemsetAsync(e->d_status.p, 0, sizeof(int), e->stream));
   WG_CK(cudaMemcpyAsync(e->w_vis.p, vel, nv * 4, cudaMemcpyHostToDevice, e->stream));
-  WG_CK(cudaMemcpyAsync(e->w_obs.p, obs, no * 4, cudaMemcpyHostToDevice, e->stream));
-  WG_TRY(gradient_dev_impl(e, e->w_vis.as<float>(), e->w_obs.as<float>(), models, e->w_loss.as<double>(),
-                           e->w_grad.as<float>(), e->stream));
+  // the observed data travel on a second stream while the first forward pass runs
+  if (!e->copy_stream) WG_CK(cudaStreamCreateWithFlags(&e->copy_stream, cudaStreamNonBlocking));
+  if (!e->obs_ready) WG_CK(cudaEventCreateWithFlags(&e->obs_ready, cudaEventDisableTiming));
+  WG_CK(cudaMemcpyAsync(e->w_obs.p, obs, no * 4, cudaMemcpyHostToDevice, e->copy_stream));
+  WG_CK(cudaEventRecord(e->obs_ready, e->copy_stream));
+  const int rc = e->streamed ? [&] {
+    const cudaError_t w = cudaStreamWaitEvent(e->stream, e->obs_ready, 0);
+    return w == cudaSuccess ? gradient_dev_impl(e, e->w_vis.as<float>(), e->w_obs.as<float>(), models,
+                                                e->w_loss.as<double>(), e->w_grad.as<float>(), e->stream)
+                            : fail(WG_ERR_CUDA, cudaGetErrorString(w));
+  }()
+                             : gradient_dev_impl(e, e->w_vis.as<float>(), e->w_obs.as<float>(), models,
+                                                 e->w_loss.as<double>(), e->w_grad.as<float>(), e->stream, e->obs_ready);
+  if (rc != WG_OK) {
+    cudaStreamSynchronize(e->copy_stream);
+    return rc;
+  }
   WG_CK(cudaMemcpyAsync(loss, e->w_loss.p, static_cast<size_t>(models) * 8, cudaMemcpyDeviceToHost, e->stream));
   WG_CK(cudaMemcpyAsync(grad, e->w_grad.p, nv * 4, cudaMemcpyDeviceToHost, e->stream));
   WG_CK(cudaStreamSynchronize(e->stream));
