@@ -314,3 +314,35 @@ def test_every_adjoint_shape_bitexact_70x70(cuda_lib, k):
             loss, grad = eng.evaluate_adjoint(cur, obs)
             np.testing.assert_array_equal(grad, rg, err_msg=f"shape {shape} prefetch {pref}")
             np.testing.assert_allclose(loss, rl, rtol=1e-12)
+
+
+def smooth_model(nz: int, nx: int, seed: int) -> np.ndarray:
+    rng = np.random.default_rng(seed)
+    zz = np.arange(nz, dtype=np.float32)[:, None]
+    xx = np.arange(nx, dtype=np.float32)[None, :]
+    v = 1800.0 + 2400.0 * zz / nz + 300.0 * np.sin(xx / 7.0 + rng.random()) * np.cos(zz / 5.0)
+    return v.astype(np.float32)
+
+
+@pytest.mark.parametrize("nxv,nzv", [(100, 100), (140, 140), (70, 50)])
+def test_every_shape_gradient_bitexact_other_grids(cuda_lib, nxv, nzv):
+    """Each compiled forward and adjoint launch shape that fits the 100x100 and 140x140 grids of
+    the data-generation batch and a 70-wide grid whose rows do not split evenly into segments."""
+    sv = o.Survey(shots=2, nt=160, dt=0.001, nx_vis=nxv, nz_vis=nzv)
+    src = np.float32([[0.0, 10.0], [(nxv - 1) * 5.0 + 2.5, 15.0]])
+    eng = make_engine(sv, src, checkpoint_every=50)
+    wav = eng.wavelet()
+    cur = np.stack([smooth_model(nzv, nxv, 1), smooth_model(nzv, nxv, 2)])
+    obs = o.forward(sv, np.stack([smooth_model(nzv, nxv, 3), smooth_model(nzv, nxv, 4)]), src, wav)
+    rl, rg = o.evaluate_adjoint(sv, cur, src, wav, obs)
+    fshapes, ashapes = eng.shape_candidates("forward"), eng.shape_candidates("adjoint")
+    assert fshapes and ashapes
+    for shape in ashapes:
+        eng.set_launch_shape("adjoint", shape)
+        loss, grad = eng.evaluate_adjoint(cur, obs)
+        np.testing.assert_array_equal(grad, rg, err_msg=f"adjoint shape {shape}")
+        np.testing.assert_allclose(loss, rl, rtol=1e-12)
+    for shape in fshapes:
+        eng.set_launch_shape("forward", shape)
+        loss, grad = eng.evaluate_adjoint(cur, obs)
+        np.testing.assert_array_equal(grad, rg, err_msg=f"forward shape {shape}")

@@ -324,7 +324,7 @@ bool pick_shapes(wg_engine* e) {
   }
   for (const auto& t : apref) {
     wg::Shape s;
-    if (find_shape(1, t[0], t[1], t[2], &s) && wg::adj_shape_fits(s, e->nx, e->nz, e->swa)) {
+    if (find_shape(1, t[0], t[1], t[2], &s) && wg::adj_shape_fits(s, e->nx, e->nz, e->swa, e->nrec)) {
       e->ashape = s;
       break;
     }
@@ -889,7 +889,7 @@ int wg_set_launch_shape(wg_engine* e, int which, int cluster, int threads, int c
     if (!wg::fwd_shape_fits(s, e->nx, e->nz, e->sw, e->nrec)) return fail(WG_ERR_ARG, "forward shape does not fit this grid");
     e->fshape = s;
   } else {
-    if (!wg::adj_shape_fits(s, e->nx, e->nz, e->swa)) return fail(WG_ERR_ARG, "adjoint shape does not fit this grid");
+    if (!wg::adj_shape_fits(s, e->nx, e->nz, e->swa, e->nrec)) return fail(WG_ERR_ARG, "adjoint shape does not fit this grid");
     e->ashape = s;
   }
   return WG_OK;
@@ -911,7 +911,7 @@ int wg_shape_candidates(const wg_engine* e, int which, int* out3, int max_shapes
   for (int i = 0; i < total; ++i) {
     const wg::Shape s = which == 0 ? wg::fwd_shape(i) : wg::adj_shape(i);
     const bool fits = which == 0 ? wg::fwd_shape_fits(s, e->nx, e->nz, e->sw, e->nrec)
-                                 : wg::adj_shape_fits(s, e->nx, e->nz, e->swa);
+                                 : wg::adj_shape_fits(s, e->nx, e->nz, e->swa, e->nrec);
     if (!fits) continue;
     if (n < max_shapes) {
       out3[3 * n] = s.cluster;

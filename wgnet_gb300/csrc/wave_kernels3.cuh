@@ -50,6 +50,18 @@ __device__ __forceinline__ int warp_role(int warp) {
   return j;
 }
 
+constexpr bool kLateStore = false;
+
+// Thread order for the per-step receiver work (trace recording, residual staging): it starts at a
+// segment away from the z strips and from the rows sent to the peer CTAs, whose warps have the
+// least to do per step.
+template <int NSEG, int NI, int C>
+__device__ __forceinline__ int light_tid(int tid, int rank) {
+  constexpr int SEGT = 32 * (1 + NI), NT = NSEG * SEGT;
+  const int ls = (C == 1) ? NSEG / 2 : (rank == 0 ? NSEG / 2 + 1 : 1);
+  return (tid - ls * SEGT + NT) % NT;
+}
+
 __device__ __forceinline__ float2 lds2(const float* p) { return *reinterpret_cast<const float2*>(p); }
 __device__ __forceinline__ void sts2(float* p, float a, float b) { *reinterpret_cast<float2*>(p) = make_float2(a, b); }
 
@@ -70,7 +82,9 @@ __global__ void __launch_bounds__(NSEG * 32 * (1 + NI), 1) fwd3_kernel(const __g
   constexpr int NT = NSEG * 32 * (1 + NI);
   extern __shared__ __align__(16) float sm[];
   const Grid& g = p.g;
-  const int nz = g.nz, sw = g.sw, region = g.region, nrec = p.st.nrec;
+  // FULL: the rows split evenly into the segments, so nz (and every layout offset) is known here
+  const int nz = FULL ? C * S * NSEG + 2 * FD_PAD : g.nz;
+  const int sw = g.sw, region = g.region, nrec = p.st.nrec;
   const float rh = g.rh, dt2 = g.dt2, d2a = g.d2a, d2b = g.d2b;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int seg = warp / (1 + NI), wk = warp_role<NI>(warp);
@@ -115,6 +129,7 @@ __global__ void __launch_bounds__(NSEG * 32 * (1 + NI), 1) fwd3_kernel(const __g
   const bool pml = (wk == 0);
   const int x = CL::x_of(wk, lane);
   const int zb = r0 + seg * S;
+  const int ltid = light_tid<NSEG, NI, C>(tid, rank);
   // FULL: every segment of every CTA has exactly S rows (checked on the host)
   const int nrows = CL::active(wk, lane) ? (FULL ? S : max(0, min(S, r1 - zb))) : 0;
   const bool pusher = (C > 1) && nrows > 0 && ((rank > 0 && zb < r0 + FD_PAD) || (rank < C - 1 && zb + nrows > r1 - FD_PAD));
@@ -139,6 +154,19 @@ __global__ void __launch_bounds__(NSEG * 32 * (1 + NI), 1) fwd3_kernel(const __g
   unsigned srcmask = 0;
   const int* sc = p.st.src_cell + 4 * shot;
   const float* vel = p.vel + static_cast<size_t>(model) * cells + gbase;
+  // Source corners: cell and the step-invariant factor (-v^2 dt^2) w of the shader's
+  // (((-v^2 dt^2) w) f); the wavelet sample of the next step is staged in F[(t + 1) & 1] by one
+  // thread before each step's barrier, so the injection reads shared memory only.
+  int* sSrcCell = reinterpret_cast<int*>(sm + L.off_src);
+  float* sSrcQ = sm + L.off_src + 4;
+  float* sF = sm + L.off_src + 8;
+  if (tid < 4) {
+    const int cell = sc[tid];
+    const float v = p.vel[static_cast<size_t>(model) * cells + cell];
+    sSrcCell[tid] = cell;
+    sSrcQ[tid] = (-(v * v * dt2)) * p.st.src_w[4 * shot + tid];
+  }
+  if (ltid == 0) sF[p.t0 & 1] = g.wavelet[p.t0];
   float* V2o = sm + L.off_v2 + (zb - r0) * NX + x;  // owner-only coefficient rows
   float* C2o = sm + L.off_c2 + (zb - r0) * NX + x;
 #pragma unroll
@@ -209,17 +237,6 @@ __global__ void __launch_bounds__(NSEG * 32 * (1 + NI), 1) fwd3_kernel(const __g
     float* APZn = APZ + (1 - par) * zstride + zbase;
     float* ZZo = ZZ + zbase;
 
-    if (TRACES) {
-      const float* Ucb = U + par * ustride;
-      for (int r = tid; r < nrec; r += NT) {
-        if (sRecOk[r]) {
-          float acc = 0.0f;
-#pragma unroll
-          for (int k = 0; k < 4; ++k) acc = acc + sRecW[4 * r + k] * Ucb[sRecCell[4 * r + k]];
-          p.traces[(static_cast<size_t>(unit) * g.nt + t) * nrec + r] = acc;
-        }
-      }
-    }
     if (p.ck_out && t > p.t0 && (t % p.ck_every) == 0) {
       float* ck = p.ck_out + (static_cast<size_t>(unit) * p.ck_slots + (t / p.ck_every - 1)) * ckf;
       float* cAX = ck + 2 * cells;
@@ -250,9 +267,9 @@ __global__ void __launch_bounds__(NSEG * 32 * (1 + NI), 1) fwd3_kernel(const __g
       }
     }
 
-    const float f = __ldg(&g.wavelet[t]);
+    const float f = sF[t & 1];
     float* st = STORE ? p.stored + (static_cast<size_t>(unit) * (p.t1 - p.t0) + (t - p.t0)) * cells + gbase : nullptr;
-    float2 stv[STORE ? S : 1];
+    float2 stv[STORE && kLateStore ? S : 1];
 #pragma unroll
     for (int i = 0; i < S; ++i) {
       if (i < nrows) {
@@ -348,7 +365,8 @@ __global__ void __launch_bounds__(NSEG * 32 * (1 + NI), 1) fwd3_kernel(const __g
         const float v20 = vv.x, v21 = vv.y;
         if (STORE) {
           const float2 cc = lds2(C2o + i * NX);
-          stv[i] = make_float2(cc.x * w0, cc.y * w1);
+          if constexpr (kLateStore) stv[kLateStore ? i : 0] = make_float2(cc.x * w0, cc.y * w1);
+          else *reinterpret_cast<float2*>(st + i * NX) = make_float2(cc.x * w0, cc.y * w1);
         }
         float n0 = ((v20 * w0) + (2.0f * u0)) - un[i][0];
         float n1 = ((v21 * w1) + (2.0f * u1)) - un[i][1];
@@ -356,9 +374,8 @@ __global__ void __launch_bounds__(NSEG * 32 * (1 + NI), 1) fwd3_kernel(const __g
           const int cell = gbase + i * NX;
 #pragma unroll
           for (int k = 0; k < 4; ++k) {
-            const float wk_ = p.st.src_w[4 * shot + k];
-            if (cell == sc[k]) n0 = n0 + (((-v20) * wk_) * f);
-            if (cell + 1 == sc[k]) n1 = n1 + (((-v21) * wk_) * f);
+            if (cell == sSrcCell[k]) n0 = n0 + (sSrcQ[k] * f);
+            if (cell + 1 == sSrcCell[k]) n1 = n1 + (sSrcQ[k] * f);
           }
         }
         un[i][0] = n0;
@@ -371,15 +388,29 @@ __global__ void __launch_bounds__(NSEG * 32 * (1 + NI), 1) fwd3_kernel(const __g
         }
       }
     }
+    if (TRACES) {
+      // receivers at time t, recorded after this thread's update by the threads with the least
+      // work per step: nothing writes buffer `par` before this step's barrier
+      const float* Ucb = U + par * ustride;
+      for (int r = ltid; r < nrec; r += NT) {
+        if (sRecOk[r]) {
+          float acc = 0.0f;
+#pragma unroll
+          for (int k = 0; k < 4; ++k) acc = acc + sRecW[4 * r + k] * Ucb[sRecCell[4 * r + k]];
+          p.traces[(static_cast<size_t>(unit) * g.nt + t) * nrec + r] = acc;
+        }
+      }
+    }
+    if (ltid == 0 && t + 1 < p.t1) sF[(t + 1) & 1] = g.wavelet[t + 1];
     if constexpr (C > 1) {
       if (pusher) fence_cluster();
       __syncthreads();
       cluster_arrive_relaxed();
     }
-    if (STORE) {  // the gradient terms go to global memory while the peers catch up
+    if constexpr (STORE && kLateStore) {  // the gradient terms go to global memory while the peers catch up
 #pragma unroll
       for (int i = 0; i < S; ++i)
-        if (i < nrows) *reinterpret_cast<float2*>(st + i * NX) = stv[i];
+        if (i < nrows) *reinterpret_cast<float2*>(st + i * NX) = stv[kLateStore ? i : 0];
     }
     if constexpr (C > 1) cluster_wait_acquire();
     else __syncthreads();
@@ -405,7 +436,8 @@ __global__ void __launch_bounds__(NSEG * 32 * (1 + NI), 1) adj3_kernel(const __g
   constexpr int NT = NSEG * 32 * (1 + NI);
   extern __shared__ __align__(16) float sm[];
   const Grid& g = p.g;
-  const int nz = g.nz, swa = g.swa, region = g.region_adj, nrec = p.st.nrec, nt = g.nt;
+  const int nz = FULL ? C * S * NSEG + 2 * FD_PAD : g.nz;  // compile-time for evenly split rows
+  const int swa = g.swa, region = g.region_adj, nrec = p.st.nrec, nt = g.nt;
   const float rh = g.rh, dt2 = g.dt2;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int seg = warp / (1 + NI), wk = warp_role<NI>(warp);
@@ -414,7 +446,7 @@ __global__ void __launch_bounds__(NSEG * 32 * (1 + NI), 1) adj3_kernel(const __g
   const int shot = unit % p.st.shots;
   const int model = unit / p.st.shots;
   const size_t cells = static_cast<size_t>(NX) * nz;
-  const A3Layout L = a3_layout_rt(NX, PMLP, nz, swa, C);
+  const A3Layout L = a3_layout_rt(NX, PMLP, nz, swa, C, nrec);
   const int r0 = split_row(nz, C, rank), r1 = split_row(nz, C, rank + 1);
   const int zl0 = r0 - FD_PAD;
   const int bot_off = (C == 1) ? swa : 0;
@@ -455,6 +487,56 @@ __global__ void __launch_bounds__(NSEG * 32 * (1 + NI), 1) adj3_kernel(const __g
   // per-column constants live in shared memory: (1 + b) in sOPB, a, b, db in the profiles
   float* sOPB = sm + L.off_opb;
   for (int i = tid; i < NX; i += NT) sOPB[i] = 1.0f + g.prof[NX + i];
+  // Source corners: cell and the step-invariant factor ((-2 v) dt^2) w of the shader's
+  // ((((-2 v) dt^2) w) f) (left to right, so the product with f rounds identically).
+  int* sSrcCell = reinterpret_cast<int*>(sm + L.off_src);
+  float* sSrcF = sm + L.off_src + 4;
+  // wavelet samples of this launch's steps, F[t - t_lo], when they fit
+  float* sF = sm + L.off_src + 8;
+  const bool wstage = p.t_hi - p.t_lo <= G3_WAV_STEPS;
+  if (wstage)
+    for (int i = tid; i < p.t_hi - p.t_lo; i += NT) sF[i] = g.wavelet[p.t_lo + i];
+  if (tid < 4) {
+    const int cell = p.st.src_cell[4 * shot + tid];
+    sSrcCell[tid] = cell;
+    sSrcF[tid] = (((-2.0f) * p.vel[static_cast<size_t>(model) * cells + cell]) * dt2) * p.st.src_w[4 * shot + tid];
+  }
+  // The receiver CSR of this CTA's rows in shared memory: up to G3_REC_ROWS rows with entries get
+  // a slot with their cells' entry offsets (relative to the CTA's first entry e0); rows beyond that
+  // read the global CSR. Per step, P[t & 1][e] = w_e * residual(t, receiver_e) (the product of the
+  // shader's injection term) is formed one step ahead, from a residual loaded two steps ahead, by
+  // one thread per entry, so the injection adds shared-memory values in CSR order.
+  int* sRRow = reinterpret_cast<int*>(sm + L.off_rrow);
+  int* sROff = reinterpret_cast<int*>(sm + L.off_roff);
+  float* sEW = sm + L.off_ew;
+  int* sER = reinterpret_cast<int*>(sm + L.off_er);
+  float* sP = sm + L.off_res;
+  const int crows = r1 - r0;
+  const int E0 = p.st.csr[r0 * NX];
+  const int ecnt = p.st.csr[r1 * NX] - E0;
+  const bool stage = ecnt <= L.pcap && ecnt <= NT;
+  const int ltid = light_tid<NSEG, NI, C>(tid, rank);
+  const float* resu = p.residual + static_cast<size_t>(unit) * nt * nrec;
+  float rnext = 0.0f;
+  if (stage && ltid < ecnt) {
+    const int rec = p.st.ent_rec[E0 + ltid];
+    const float w = p.st.ent_w[E0 + ltid];
+    sEW[ltid] = w;
+    sER[ltid] = rec;
+    sP[((p.t_hi - 1) & 1) * L.pcap + ltid] = w * resu[static_cast<size_t>(p.t_hi - 1) * nrec + rec];
+    if (p.t_hi - 2 >= p.t_lo) rnext = resu[static_cast<size_t>(p.t_hi - 2) * nrec + rec];
+  }
+  if (warp == 0) {
+    int used = 0;
+    for (int c0 = 0; c0 < crows; c0 += 32) {
+      const int r = c0 + lane;
+      const bool has = r < crows && p.st.csr[(r0 + r) * NX] < p.st.csr[(r0 + r + 1) * NX];
+      const unsigned b = __ballot_sync(0xffffffffu, has);
+      const int slot = used + __popc(b & ((1u << lane) - 1u));
+      if (r < crows) sRRow[r] = (has && stage && slot < G3_REC_ROWS) ? slot : -1;
+      used += __popc(b);
+    }
+  }
 
   float lA[S][2], lB[S][2];
   unsigned srcmask = 0, recmask = 0;
@@ -470,8 +552,17 @@ __global__ void __launch_bounds__(NSEG * 32 * (1 + NI), 1) adj3_kernel(const __g
   float* sZZ = sPZ + static_cast<size_t>(2) * swa * NX;
   float* gacc = p.gacc + static_cast<size_t>(unit) * cells + gbase;
   __syncthreads();
+  for (int i = tid; i < crows * (NX + 1); i += NT) {
+    const int r = i / (NX + 1), xx = i - r * (NX + 1), slot = sRRow[r];
+    if (slot >= 0) sROff[slot * (NX + 4) + xx] = p.st.csr[(r0 + r) * NX + xx] - E0;
+  }
+  unsigned recslots = 0;  // per own row: 3 bits, the row's slot or 7 (global CSR)
 #pragma unroll
   for (int i = 0; i < S; ++i) {
+    if (i < nrows) {
+      const int slot = sRRow[zb - r0 + i];
+      recslots |= static_cast<unsigned>(slot >= 0 ? slot : 7) << (3 * i);
+    }
 #pragma unroll
     for (int j = 0; j < 2; ++j) lA[i][j] = lB[i][j] = 0.f;
     if (i < nrows) {
@@ -510,10 +601,23 @@ __global__ void __launch_bounds__(NSEG * 32 * (1 + NI), 1) adj3_kernel(const __g
 
   const int pr_lo = (rank > 0) ? split_row(nz, C, rank - 1) - FD_PAD : 0;
 
-  // Derived terms of this thread's cells for lambda `lc`: VS into buffer b, the strip terms into
-  // their single buffers.
-  auto derive = [&](int b, const float (&lc)[S][2]) {
+  // VS = v^2 dt^2 lambda of row i into buffer b (and into the peer CTA's halo rows).
+  auto put_vs = [&](int b, int i, float l0, float l1) {
     float* VSb = sm + L.off_vs + b * vstride;
+    const int z = zb + i;
+    const float2 v2 = lds2(V2o + i * NX);
+    const float vs0 = v2.x * l0;
+    const float vs1 = v2.y * l1;
+    sts2(VSb + vbase + i * NX, vs0, vs1);
+    if constexpr (C > 1) {
+      if (rank > 0 && z < r0 + FD_PAD) st_peer_v2(VSb + (z - pr_lo) * NX + x, rank - 1, vs0, vs1);
+      if (rank < C - 1 && z >= r1 - FD_PAD) st_peer_v2(VSb + (z - (r1 - FD_PAD)) * NX + x, rank + 1, vs0, vs1);
+    }
+  };
+  // Strip terms T = (1 + b) VS + b zeta and U1 = db T + b psi of this thread's cells from VS in
+  // buffer b, into their single buffers.
+  auto derive_strips = [&](int b) {
+    const float* VSb = sm + L.off_vs + b * vstride;
     float* TXb = TXs;
     float* U1Xb = U1Xs;
     float* TZb = TZs;
@@ -522,14 +626,10 @@ __global__ void __launch_bounds__(NSEG * 32 * (1 + NI), 1) adj3_kernel(const __g
     for (int i = 0; i < S; ++i) {
       if (i < nrows) {
         const int z = zb + i;
-        const float2 v2 = lds2(V2o + i * NX);
-        const float vs0 = v2.x * lc[i][0];
-        const float vs1 = v2.y * lc[i][1];
-        sts2(VSb + vbase + i * NX, vs0, vs1);
-        if constexpr (C > 1) {
-          if (rank > 0 && z < r0 + FD_PAD) st_peer_v2(VSb + (z - pr_lo) * NX + x, rank - 1, vs0, vs1);
-          if (rank < C - 1 && z >= r1 - FD_PAD) st_peer_v2(VSb + (z - (r1 - FD_PAD)) * NX + x, rank + 1, vs0, vs1);
-        }
+        const bool zstrip = z < swa || z >= nz - swa;
+        if (!(pml || xedge || zstrip)) continue;
+        const float2 vs = lds2(VSb + vbase + i * NX);
+        const float vs0 = vs.x, vs1 = vs.y;
         if (pml || xedge) {
           // outside the adjoint region (xedge) b = db = 0 and the adjoint psi, zeta are zero
           const float2 o = lds2(sOPB + x), b = lds2(sBX + x), db = lds2(sDBX + x);
@@ -540,7 +640,7 @@ __global__ void __launch_bounds__(NSEG * 32 * (1 + NI), 1) adj3_kernel(const __g
           sts2(TXb + i * 2 * SW, T0, T1);
           sts2(U1Xb + i * 2 * SW, (db.x * T0) + (b.x * P.x), (db.y * T1) + (b.y * P.y));
         }
-        if (z < swa || z >= nz - swa) {
+        if (zstrip) {
           const float bz = sBZ[z], dbz = sDBZ[z];
           const float opbz = 1.0f + bz;
           const float2 Z = lds2(LZZ + i * NX);
@@ -554,7 +654,10 @@ __global__ void __launch_bounds__(NSEG * 32 * (1 + NI), 1) adj3_kernel(const __g
     }
   };
 
-  derive(0, lA);
+#pragma unroll
+  for (int i = 0; i < S; ++i)
+    if (i < nrows) put_vs(0, i, lA[i][0], lA[i][1]);
+  derive_strips(0);  // reads only this thread's own VS cells
   step_barrier<C>();
 
   const int segn = p.t_hi - p.t_lo;
@@ -575,7 +678,7 @@ __global__ void __launch_bounds__(NSEG * 32 * (1 + NI), 1) adj3_kernel(const __g
     const float* U1Xd = U1Xs;
     const float* TZd = TZs;
     const float* U1Zd = U1Zs;
-    const float f = __ldg(&g.wavelet[t]);
+    const float f = wstage ? sF[t - p.t_lo] : __ldg(&g.wavelet[t]);
     const float* res_t = p.residual + (static_cast<size_t>(unit) * nt + t) * nrec;
     const float* st_t = p.stored + (static_cast<size_t>(unit) * segn + (t - p.t_lo)) * cells + gbase;
 #pragma unroll
@@ -647,19 +750,27 @@ __global__ void __launch_bounds__(NSEG * 32 * (1 + NI), 1) adj3_kernel(const __g
         float g0 = (lc[i][0] * sv.x) * 1.0f;
         float g1 = (lc[i][1] * sv.y) * 1.0f;
         if (recmask & (3u << (2 * i))) {
-          const int cell = gbase + i * NX;
-          const int e1 = p.st.csr[cell + 1], e2 = p.st.csr[cell + 2];
-          for (int e = p.st.csr[cell]; e < e1; ++e) n0 = n0 + (p.st.ent_w[e] * res_t[p.st.ent_rec[e]]);
-          for (int e = e1; e < e2; ++e) n1 = n1 + (p.st.ent_w[e] * res_t[p.st.ent_rec[e]]);
+          const unsigned slot = (recslots >> (3 * i)) & 7u;
+          if (slot < G3_REC_ROWS) {
+            const int* o = sROff + slot * (NX + 4) + x;
+            const float* P = sP + (t & 1) * L.pcap;
+            const int e0 = o[0], e1 = o[1], e2 = o[2];
+            for (int e = e0; e < e1; ++e) n0 = n0 + P[e];
+            for (int e = e1; e < e2; ++e) n1 = n1 + P[e];
+          } else {
+            const int cell = gbase + i * NX;
+            const int e1 = p.st.csr[cell + 1], e2 = p.st.csr[cell + 2];
+            for (int e = p.st.csr[cell]; e < e1; ++e) n0 = n0 + (p.st.ent_w[e] * res_t[p.st.ent_rec[e]]);
+            for (int e = e1; e < e2; ++e) n1 = n1 + (p.st.ent_w[e] * res_t[p.st.ent_rec[e]]);
+          }
         }
+        if (t > p.t_lo) put_vs(1 - par, i, n0, n1);  // VS of the new lambda for step t - 1
         if (srcmask & (3u << (2 * i))) {
           const int cell = gbase + i * NX;
-          const float2 v = __ldg(reinterpret_cast<const float2*>(vel + i * NX));
 #pragma unroll
           for (int k = 0; k < 4; ++k) {
-            const float wk_ = p.st.src_w[4 * shot + k];
-            if (cell == sc[k]) g0 = g0 + lc[i][0] * (((((-2.0f) * v.x) * dt2) * wk_) * f);
-            if (cell + 1 == sc[k]) g1 = g1 + lc[i][1] * (((((-2.0f) * v.y) * dt2) * wk_) * f);
+            if (cell == sSrcCell[k]) g0 = g0 + lc[i][0] * (sSrcF[k] * f);
+            if (cell + 1 == sSrcCell[k]) g1 = g1 + lc[i][1] * (sSrcF[k] * f);
           }
         }
         {
@@ -672,13 +783,15 @@ __global__ void __launch_bounds__(NSEG * 32 * (1 + NI), 1) adj3_kernel(const __g
     }
     if (t > p.t_lo) {
       __syncthreads();  // every read of the single-buffered strip terms of step t is done
-      derive(1 - par, lp);
+      derive_strips(1 - par);
+      if (stage && ltid < ecnt) sP[((t - 1) & 1) * L.pcap + ltid] = sEW[ltid] * rnext;
     }
     if constexpr (C > 1) {
       if (pusher) fence_cluster();
       __syncthreads();
       cluster_arrive_relaxed();
     }
+    if (stage && ltid < ecnt && t - 2 >= p.t_lo) rnext = resu[static_cast<size_t>(t - 2) * nrec + sER[ltid]];
     if (PREF && t > p.t_lo) {  // next step's stored terms, fetched while the peers catch up
       const float* stn = p.stored + (static_cast<size_t>(unit) * segn + (t - 1 - p.t_lo)) * cells + gbase;
 #pragma unroll

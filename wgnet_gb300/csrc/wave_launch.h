@@ -18,9 +18,9 @@ int adj_shape_count();
 Shape fwd_shape(int i);
 Shape adj_shape(int i);
 size_t fwd_smem_bytes(const Shape& s, int nx, int nz, int sw, int nrec);
-size_t adj_smem_bytes(const Shape& s, int nx, int nz, int swa);
+size_t adj_smem_bytes(const Shape& s, int nx, int nz, int swa, int nrec);
 bool fwd_shape_fits(const Shape& s, int nx, int nz, int sw, int nrec);
-bool adj_shape_fits(const Shape& s, int nx, int nz, int swa);
+bool adj_shape_fits(const Shape& s, int nx, int nz, int swa, int nrec);
 
 // Per-shape launchers, specialised in the wave_inst_*.cu files.
 template <int C, int NT, int CPT>

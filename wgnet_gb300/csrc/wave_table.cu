@@ -57,8 +57,9 @@ size_t fwd_smem_bytes(const Shape& s, int nx, int nz, int sw, int nrec) {
   if (s.kind == 3) return static_cast<size_t>(f3_layout_rt(s.nxc, s.pmlp, nz, sw, s.cluster, nrec).total) * sizeof(float);
   return static_cast<size_t>(fwd_layout(nx, nz, sw, s.cluster, nrec).total) * sizeof(float);
 }
-size_t adj_smem_bytes(const Shape& s, int nx, int nz, int swa) {
-  if (s.kind == 3) return static_cast<size_t>(a3_layout_rt(s.nxc, s.pmlp, nz, swa, s.cluster).total) * sizeof(float);
+size_t adj_smem_bytes(const Shape& s, int nx, int nz, int swa, int nrec) {
+  if (s.kind == 3)
+    return static_cast<size_t>(a3_layout_rt(s.nxc, s.pmlp, nz, swa, s.cluster, nrec).total) * sizeof(float);
   return static_cast<size_t>(adj_layout(nx, nz, swa, s.cluster).total) * sizeof(float);
 }
 
@@ -89,7 +90,7 @@ bool fwd_shape_fits(const Shape& s, int nx, int nz, int sw, int nrec) {
   return nx < 65536 && nz < 32768;
 }
 
-bool adj_shape_fits(const Shape& s, int nx, int nz, int swa) {
+bool adj_shape_fits(const Shape& s, int nx, int nz, int swa, int nrec) {
   if (nx < 2 * swa || nz < 2 * swa) return false;
   const int rows = max_rows(nz, s.cluster);
   if (s.kind == 3) {
@@ -97,7 +98,7 @@ bool adj_shape_fits(const Shape& s, int nx, int nz, int swa) {
   } else if (static_cast<long>(rows) * (nx - 2 * FD_PAD) > static_cast<long>(s.threads) * s.cpt) {
     return false;
   }
-  if (adj_smem_bytes(s, nx, nz, swa) > kMaxSmemPerCta) return false;
+  if (adj_smem_bytes(s, nx, nz, swa, nrec) > kMaxSmemPerCta) return false;
   if (s.cluster > 1) {
     if (split_row(nz, s.cluster, 1) < swa || split_row(nz, s.cluster, s.cluster - 1) > nz - swa) return false;
   }
@@ -122,7 +123,7 @@ cudaError_t launch_fwd(const Shape& s, bool traces, bool store, const FwdArgs& a
 }
 
 cudaError_t launch_adj(const Shape& s, const AdjArgs& a, cudaStream_t stream) {
-  const size_t smem = adj_smem_bytes(s, a.g.nx, a.g.nz, a.g.swa);
+  const size_t smem = adj_smem_bytes(s, a.g.nx, a.g.nz, a.g.swa, a.st.nrec);
   if (s.kind == 3) {
 #define WG_ADJ3(NXs, PMLPs, Cc, Ss, NSEGs, NIs)                                                                  \
   if (s.nxc == NXs && s.pmlp == PMLPs && s.cluster == Cc && s.seg_rows == Ss && s.nseg == NSEGs && s.ni == NIs) \
