@@ -221,6 +221,8 @@ __global__ void __launch_bounds__(NSEG * 32 * (1 + NI), 1) fwd3_kernel(const __g
       }
     }
   }
+  // rows where any lane of the warp injects the source: warp-uniform branches, per-lane selects
+  const unsigned wsrc = __reduce_or_sync(0xffffffffu, srcmask);
   if constexpr (C > 1) cluster_barrier();
   else __syncthreads();
 
@@ -370,12 +372,15 @@ __global__ void __launch_bounds__(NSEG * 32 * (1 + NI), 1) fwd3_kernel(const __g
         }
         float n0 = ((v20 * w0) + (2.0f * u0)) - un[i][0];
         float n1 = ((v21 * w1) + (2.0f * u1)) - un[i][1];
-        if (srcmask & (3u << (2 * i))) {
+        if (wsrc & (3u << (2 * i))) {
           const int cell = gbase + i * NX;
 #pragma unroll
           for (int k = 0; k < 4; ++k) {
-            if (cell == sSrcCell[k]) n0 = n0 + (sSrcQ[k] * f);
-            if (cell + 1 == sSrcCell[k]) n1 = n1 + (sSrcQ[k] * f);
+            const int c = sSrcCell[k];
+            const float q = sSrcQ[k] * f;
+            const float a0 = n0 + q, a1 = n1 + q;
+            n0 = (cell == c) ? a0 : n0;
+            n1 = (cell + 1 == c) ? a1 : n1;
           }
         }
         un[i][0] = n0;
@@ -596,6 +601,9 @@ __global__ void __launch_bounds__(NSEG * 32 * (1 + NI), 1) adj3_kernel(const __g
       }
     }
   }
+  // rows where any lane of the warp injects a residual or the source: warp-uniform branches
+  const unsigned wrec = __reduce_or_sync(0xffffffffu, recmask);
+  const unsigned wsrc = __reduce_or_sync(0xffffffffu, srcmask);
   if constexpr (C > 1) cluster_barrier();
   else __syncthreads();
 
@@ -749,7 +757,7 @@ __global__ void __launch_bounds__(NSEG * 32 * (1 + NI), 1) adj3_kernel(const __g
         // only in the sign of an exact zero
         float g0 = (lc[i][0] * sv.x) * 1.0f;
         float g1 = (lc[i][1] * sv.y) * 1.0f;
-        if (recmask & (3u << (2 * i))) {
+        if (wrec & (3u << (2 * i))) {  // cells without entries have empty ranges
           const unsigned slot = (recslots >> (3 * i)) & 7u;
           if (slot < G3_REC_ROWS) {
             const int* o = sROff + slot * (NX + 4) + x;
@@ -765,12 +773,15 @@ __global__ void __launch_bounds__(NSEG * 32 * (1 + NI), 1) adj3_kernel(const __g
           }
         }
         if (t > p.t_lo) put_vs(1 - par, i, n0, n1);  // VS of the new lambda for step t - 1
-        if (srcmask & (3u << (2 * i))) {
+        if (wsrc & (3u << (2 * i))) {
           const int cell = gbase + i * NX;
 #pragma unroll
           for (int k = 0; k < 4; ++k) {
-            if (cell == sSrcCell[k]) g0 = g0 + lc[i][0] * (sSrcF[k] * f);
-            if (cell + 1 == sSrcCell[k]) g1 = g1 + lc[i][1] * (sSrcF[k] * f);
+            const int c = sSrcCell[k];
+            const float q = sSrcF[k] * f;
+            const float a0 = g0 + lc[i][0] * q, a1 = g1 + lc[i][1] * q;
+            g0 = (cell == c) ? a0 : g0;
+            g1 = (cell + 1 == c) ? a1 : g1;
           }
         }
         {
