@@ -75,15 +75,17 @@ __device__ __forceinline__ void st_peer_v2(const float* local_ptr, unsigned peer
 // ------------------------------------------------------------------------------------------------
 // Forward (splatForward.wgsl:48-121)
 // ------------------------------------------------------------------------------------------------
-template <int NX, int PMLP, int C, int S, int NSEG, int NI, bool FULL, bool TRACES, bool STORE>
+// SQ: the grid is square (nz = NX), so nz and every shared-memory offset are compile-time constants;
+// FULL: besides, the rows split evenly into the segments (every segment has exactly S rows).
+template <int NX, int PMLP, int C, int S, int NSEG, int NI, bool SQ, bool TRACES, bool STORE>
 __global__ void __launch_bounds__(NSEG * 32 * (1 + NI), 1) fwd3_kernel(const __grid_constant__ FwdArgs p) {
   using CL = Cols3<NX, PMLP>;
   constexpr int SW = CL::SW;
   constexpr int NT = NSEG * 32 * (1 + NI);
   extern __shared__ __align__(16) float sm[];
   const Grid& g = p.g;
-  // FULL: the rows split evenly into the segments, so nz (and every layout offset) is known here
-  const int nz = FULL ? C * S * NSEG + 2 * FD_PAD : g.nz;
+  constexpr bool FULL = SQ && (NX - 2 * FD_PAD == C * S * NSEG);
+  const int nz = SQ ? NX : g.nz;
   const int sw = g.sw, region = g.region, nrec = p.st.nrec;
   const float rh = g.rh, dt2 = g.dt2, d2a = g.d2a, d2b = g.d2b;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -130,7 +132,6 @@ __global__ void __launch_bounds__(NSEG * 32 * (1 + NI), 1) fwd3_kernel(const __g
   const int x = CL::x_of(wk, lane);
   const int zb = r0 + seg * S;
   const int ltid = light_tid<NSEG, NI, C>(tid, rank);
-  // FULL: every segment of every CTA has exactly S rows (checked on the host)
   const int nrows = CL::active(wk, lane) ? (FULL ? S : max(0, min(S, r1 - zb))) : 0;
   const bool pusher = (C > 1) && nrows > 0 && ((rank > 0 && zb < r0 + FD_PAD) || (rank < C - 1 && zb + nrows > r1 - FD_PAD));
   const int ubase = (zb - zl0) * NX + x;                 // row 0 of the segment in U
@@ -434,14 +435,15 @@ __global__ void __launch_bounds__(NSEG * 32 * (1 + NI), 1) fwd3_kernel(const __g
 // ------------------------------------------------------------------------------------------------
 // PREF: fetch the next step's stored gradient terms between the barrier's arrive and wait (2 S more
 // registers per thread) instead of loading each row's terms when the row is processed.
-template <int NX, int PMLP, int C, int S, int NSEG, int NI, bool FULL, bool PREF>
+template <int NX, int PMLP, int C, int S, int NSEG, int NI, bool SQ, bool PREF>
 __global__ void __launch_bounds__(NSEG * 32 * (1 + NI), 1) adj3_kernel(const __grid_constant__ AdjArgs p) {
   using CL = Cols3<NX, PMLP>;
   constexpr int SW = CL::SW;
   constexpr int NT = NSEG * 32 * (1 + NI);
   extern __shared__ __align__(16) float sm[];
   const Grid& g = p.g;
-  const int nz = FULL ? C * S * NSEG + 2 * FD_PAD : g.nz;  // compile-time for evenly split rows
+  constexpr bool FULL = SQ && (NX - 2 * FD_PAD == C * S * NSEG);  // every segment has S rows
+  const int nz = SQ ? NX : g.nz;                                  // compile-time for square grids
   const int swa = g.swa, region = g.region_adj, nrec = p.st.nrec, nt = g.nt;
   const float rh = g.rh, dt2 = g.dt2;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -850,18 +852,10 @@ __global__ void __launch_bounds__(NSEG * 32 * (1 + NI), 1) adj3_kernel(const __g
   }
 }
 
-// Every segment of every CTA has exactly S rows when the CTAs' rows split evenly into NSEG segments.
-template <int C, int S, int NSEG>
-inline bool g3_full(int nz) {
-  for (int r = 0; r < C; ++r)
-    if (split_row(nz, C, r + 1) - split_row(nz, C, r) != S * NSEG) return false;
-  return true;
-}
-
 template <int NX, int PMLP, int C, int S, int NSEG, int NI>
 cudaError_t fwd3_dispatch_impl(bool traces, bool store, const FwdArgs& a, size_t smem, cudaStream_t s) {
   constexpr int NT = NSEG * 32 * (1 + NI);
-  if (g3_full<C, S, NSEG>(a.g.nz)) {
+  if (a.g.nz == NX) {  // square grid: the compile-time layout
     if (traces && store)
       return launch_cluster(fwd3_kernel<NX, PMLP, C, S, NSEG, NI, true, true, true>, C, NT, a.units, smem, s, a);
     if (traces)
@@ -882,7 +876,7 @@ cudaError_t fwd3_dispatch_impl(bool traces, bool store, const FwdArgs& a, size_t
 template <int NX, int PMLP, int C, int S, int NSEG, int NI, bool PREF>
 cudaError_t adj3_dispatch_impl(const AdjArgs& a, size_t smem, cudaStream_t s) {
   constexpr int NT = NSEG * 32 * (1 + NI);
-  if (g3_full<C, S, NSEG>(a.g.nz))
+  if (a.g.nz == NX)
     return launch_cluster(adj3_kernel<NX, PMLP, C, S, NSEG, NI, true, PREF>, C, NT, a.units, smem, s, a);
   return launch_cluster(adj3_kernel<NX, PMLP, C, S, NSEG, NI, false, PREF>, C, NT, a.units, smem, s, a);
 }
