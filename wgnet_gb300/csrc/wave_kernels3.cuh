@@ -626,43 +626,50 @@ __global__ void __launch_bounds__(NSEG * 32 * (1 + NI), 1) adj3_kernel(const __g
   };
   // Strip terms T = (1 + b) VS + b zeta and U1 = db T + b psi of this thread's cells from VS in
   // buffer b, into their single buffers.
+  // The strip arrays are written only through the restrict-qualified pointers of `put`, so the
+  // compiler may issue every row's loads ahead of the earlier rows' stores; the per-column
+  // profile values are loaded once.
   auto derive_strips = [&](int b) {
     const float* VSb = sm + L.off_vs + b * vstride;
-    float* TXb = TXs;
-    float* U1Xb = U1Xs;
-    float* TZb = TZs;
-    float* U1Zb = U1Zs;
+    auto put = [&](float* __restrict__ TXb, float* __restrict__ U1Xb, float* __restrict__ TZb,
+                   float* __restrict__ U1Zb) {
+      const bool xs = pml || xedge;
+      // outside the adjoint region (xedge) b = db = 0 and the adjoint psi, zeta are zero
+      const float2 o = xs ? lds2(sOPB + x) : make_float2(0.f, 0.f);
+      const float2 bx = xs ? lds2(sBX + x) : make_float2(0.f, 0.f);
+      const float2 db = xs ? lds2(sDBX + x) : make_float2(0.f, 0.f);
 #pragma unroll
-    for (int i = 0; i < S; ++i) {
-      if (i < nrows) {
-        const int z = zb + i;
-        const bool zstrip = z < swa || z >= nz - swa;
-        if (!(pml || xedge || zstrip)) continue;
-        const float2 vs = lds2(VSb + vbase + i * NX);
-        const float vs0 = vs.x, vs1 = vs.y;
-        if (pml || xedge) {
-          // outside the adjoint region (xedge) b = db = 0 and the adjoint psi, zeta are zero
-          const float2 o = lds2(sOPB + x), b = lds2(sBX + x), db = lds2(sDBX + x);
-          const float2 Z = pml ? lds2(LZX + i * 2 * SW) : make_float2(0.f, 0.f);
-          const float2 P = pml ? lds2(LPX + i * 2 * SW) : make_float2(0.f, 0.f);
-          const float T0 = (o.x * vs0) + (b.x * Z.x);
-          const float T1 = (o.y * vs1) + (b.y * Z.y);
-          sts2(TXb + i * 2 * SW, T0, T1);
-          sts2(U1Xb + i * 2 * SW, (db.x * T0) + (b.x * P.x), (db.y * T1) + (b.y * P.y));
-        }
-        if (zstrip) {
-          const float bz = sBZ[z], dbz = sDBZ[z];
-          const float opbz = 1.0f + bz;
-          const float2 Z = lds2(LZZ + i * NX);
-          const float2 P = lds2(LPZ + i * NX);
-          const float T0 = (opbz * vs0) + (bz * Z.x);
-          const float T1 = (opbz * vs1) + (bz * Z.y);
-          sts2(TZb + i * NX, T0, T1);
-          sts2(U1Zb + i * NX, (dbz * T0) + (bz * P.x), (dbz * T1) + (bz * P.y));
+      for (int i = 0; i < S; ++i) {
+        if (i < nrows) {
+          const int z = zb + i;
+          const bool zstrip = z < swa || z >= nz - swa;
+          if (!(xs || zstrip)) continue;
+          const float2 vs = lds2(VSb + vbase + i * NX);
+          const float vs0 = vs.x, vs1 = vs.y;
+          if (xs) {
+            const float2 Z = pml ? lds2(LZX + i * 2 * SW) : make_float2(0.f, 0.f);
+            const float2 P = pml ? lds2(LPX + i * 2 * SW) : make_float2(0.f, 0.f);
+            const float T0 = (o.x * vs0) + (bx.x * Z.x);
+            const float T1 = (o.y * vs1) + (bx.y * Z.y);
+            sts2(TXb + i * 2 * SW, T0, T1);
+            sts2(U1Xb + i * 2 * SW, (db.x * T0) + (bx.x * P.x), (db.y * T1) + (bx.y * P.y));
+          }
+          if (zstrip) {
+            const float bz = sBZ[z], dbz = sDBZ[z];
+            const float opbz = 1.0f + bz;
+            const float2 Z = lds2(LZZ + i * NX);
+            const float2 P = lds2(LPZ + i * NX);
+            const float T0 = (opbz * vs0) + (bz * Z.x);
+            const float T1 = (opbz * vs1) + (bz * Z.y);
+            sts2(TZb + i * NX, T0, T1);
+            sts2(U1Zb + i * NX, (dbz * T0) + (bz * P.x), (dbz * T1) + (bz * P.y));
+          }
         }
       }
-    }
+    };
+    put(TXs, U1Xs, TZs, U1Zs);
   };
+
 
 #pragma unroll
   for (int i = 0; i < S; ++i)
