@@ -65,11 +65,15 @@ __device__ __forceinline__ int light_tid(int tid, int rank) {
 __device__ __forceinline__ float2 lds2(const float* p) { return *reinterpret_cast<const float2*>(p); }
 __device__ __forceinline__ void sts2(float* p, float a, float b) { *reinterpret_cast<float2*>(p) = make_float2(a, b); }
 
+// Store to the peer CTA's copy of a shared array. The address translation is a pure function; the
+// store has no memory clobber, so it does not pin this thread's other shared-memory accesses, none
+// of which touch the peer's copy. It stays ahead of the step's cluster fence and barrier because
+// those are volatile asm too.
 __device__ __forceinline__ void st_peer_v2(const float* local_ptr, unsigned peer, float a, float b) {
   unsigned la = static_cast<unsigned>(__cvta_generic_to_shared(local_ptr));
   unsigned ra;
-  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(ra) : "r"(la), "r"(peer));
-  asm volatile("st.shared::cluster.v2.f32 [%0], {%1, %2};" ::"r"(ra), "f"(a), "f"(b) : "memory");
+  asm("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(ra) : "r"(la), "r"(peer));
+  asm volatile("st.shared::cluster.v2.f32 [%0], {%1, %2};" ::"r"(ra), "f"(a), "f"(b));
 }
 
 // ------------------------------------------------------------------------------------------------
@@ -273,127 +277,133 @@ __global__ void __launch_bounds__(NSEG * 32 * (1 + NI), 1) fwd3_kernel(const __g
     const float f = sF[t & 1];
     float* st = STORE ? p.stored + (static_cast<size_t>(unit) * (p.t1 - p.t0) + (t - p.t0)) * cells + gbase : nullptr;
     float2 stv[STORE && kLateStore ? S : 1];
+    // The row updates write only through these restrict-qualified pointers (disjoint arrays), so
+    // the compiler may issue a row's loads ahead of the previous row's stores.
+    auto rows = [&](float* __restrict__ uw, float* __restrict__ apxn, float* __restrict__ zxo,
+                    float* __restrict__ apzn, float* __restrict__ zzo, float* __restrict__ stg) {
 #pragma unroll
-    for (int i = 0; i < S; ++i) {
-      if (i < nrows) {
-        const int z = zb + i;
-        const float2 A = lds2(Uc + i * NX - 2);
-        const float2 B = lds2(Uc + i * NX + 2);
-        float zm2[2], zm1[2], zp1[2], zp2[2];
-        if (i >= 2) {
-          zm2[0] = uc[i - 2][0];
-          zm2[1] = uc[i - 2][1];
-        } else {
-          const float2 q = lds2(Uc + (i - 2) * NX);
-          zm2[0] = q.x;
-          zm2[1] = q.y;
-        }
-        if (i >= 1) {
-          zm1[0] = uc[i - 1][0];
-          zm1[1] = uc[i - 1][1];
-        } else {
-          const float2 q = lds2(Uc + (i - 1) * NX);
-          zm1[0] = q.x;
-          zm1[1] = q.y;
-        }
-        if (i + 1 < S && (FULL || i + 1 < nrows)) {
-          zp1[0] = uc[i + 1 < S ? i + 1 : i][0];
-          zp1[1] = uc[i + 1 < S ? i + 1 : i][1];
-        } else {
-          const float2 q = lds2(Uc + (i + 1) * NX);
-          zp1[0] = q.x;
-          zp1[1] = q.y;
-        }
-        if (i + 2 < S && (FULL || i + 2 < nrows)) {
-          zp2[0] = uc[i + 2 < S ? i + 2 : i][0];
-          zp2[1] = uc[i + 2 < S ? i + 2 : i][1];
-        } else {
-          const float2 q = lds2(Uc + (i + 2) * NX);
-          zp2[0] = q.x;
-          zp2[1] = q.y;
-        }
-        const float u0 = uc[i][0], u1 = uc[i][1];
-        const float d2x0 = (((F_D2A * u0 + F_D2B * (u1 + A.y)) - F_D2C * (B.x + A.x)) * d2a) * d2b;
-        const float d2x1 = (((F_D2A * u1 + F_D2B * (B.x + u0)) - F_D2C * (B.y + A.y)) * d2a) * d2b;
-        float w0, w1;
-        if (pml) {
-          const float2 P0 = lds2(APXc + i * 2 * SW - 2);
-          const float2 P1 = lds2(APXc + i * 2 * SW);
-          const float2 P2 = lds2(APXc + i * 2 * SW + 2);
-          const float2 Z = lds2(ZXo + i * 2 * SW);
-          const float d10 = ((F_D1A * (u1 - A.y)) - F_D1B * (B.x - A.x)) * rh;
-          const float d11 = ((F_D1A * (B.x - u0)) - F_D1B * (B.y - A.y)) * rh;
-          const float da0 = ((F_D1A * (P1.y - P0.y)) - F_D1B * (P2.x - P0.x)) * rh;
-          const float da1 = ((F_D1A * (P2.x - P1.x)) - F_D1B * (P2.y - P0.y)) * rh;
-          const float tmp0 = ((opbx0 * d2x0) + (dbx0 * d10)) + da0;
-          const float tmp1 = ((opbx1 * d2x1) + (dbx1 * d11)) + da1;
-          w0 = (opbx0 * tmp0) + (ax0 * Z.x);
-          w1 = (opbx1 * tmp1) + (ax1 * Z.y);
-          const float psi0 = (bx0 * d10) + P1.x;
-          const float psi1 = (bx1 * d11) + P1.y;
-          sts2(ZXo + i * 2 * SW, (bx0 * tmp0) + (ax0 * Z.x), (bx1 * tmp1) + (ax1 * Z.y));
-          sts2(APXn + i * 2 * SW, ax0 * psi0, ax1 * psi1);
-        } else {
-          w0 = d2x0;
-          w1 = d2x1;
-        }
-        const float d2z0 = (((F_D2A * u0 + F_D2B * (zp1[0] + zm1[0])) - F_D2C * (zp2[0] + zm2[0])) * d2a) * d2b;
-        const float d2z1 = (((F_D2A * u1 + F_D2B * (zp1[1] + zm1[1])) - F_D2C * (zp2[1] + zm2[1])) * d2a) * d2b;
-        if (z < region || z >= nz - region) {
-          const float az = sAZ[z], bz = sBZ[z], dbz = sDBZ[z];
-          const float opbz = 1.0f + bz;
-          const float2 Qm2 = lds2(APZc + (i - 2) * NX);
-          const float2 Qm1 = lds2(APZc + (i - 1) * NX);
-          const float2 Q0 = lds2(APZc + i * NX);
-          const float2 Qp1 = lds2(APZc + (i + 1) * NX);
-          const float2 Qp2 = lds2(APZc + (i + 2) * NX);
-          const float2 Z = lds2(ZZo + i * NX);
-          const float d10 = ((F_D1A * (zp1[0] - zm1[0])) - F_D1B * (zp2[0] - zm2[0])) * rh;
-          const float d11 = ((F_D1A * (zp1[1] - zm1[1])) - F_D1B * (zp2[1] - zm2[1])) * rh;
-          const float da0 = ((F_D1A * (Qp1.x - Qm1.x)) - F_D1B * (Qp2.x - Qm2.x)) * rh;
-          const float da1 = ((F_D1A * (Qp1.y - Qm1.y)) - F_D1B * (Qp2.y - Qm2.y)) * rh;
-          const float tmp0 = ((opbz * d2z0) + (dbz * d10)) + da0;
-          const float tmp1 = ((opbz * d2z1) + (dbz * d11)) + da1;
-          w0 = w0 + ((opbz * tmp0) + (az * Z.x));
-          w1 = w1 + ((opbz * tmp1) + (az * Z.y));
-          const float psi0 = (bz * d10) + Q0.x;
-          const float psi1 = (bz * d11) + Q0.y;
-          sts2(ZZo + i * NX, (bz * tmp0) + (az * Z.x), (bz * tmp1) + (az * Z.y));
-          sts2(APZn + i * NX, az * psi0, az * psi1);
-        } else {
-          w0 = w0 + d2z0;
-          w1 = w1 + d2z1;
-        }
-        const float2 vv = lds2(V2o + i * NX);
-        const float v20 = vv.x, v21 = vv.y;
-        if (STORE) {
-          const float2 cc = lds2(C2o + i * NX);
-          if constexpr (kLateStore) stv[kLateStore ? i : 0] = make_float2(cc.x * w0, cc.y * w1);
-          else *reinterpret_cast<float2*>(st + i * NX) = make_float2(cc.x * w0, cc.y * w1);
-        }
-        float n0 = ((v20 * w0) + (2.0f * u0)) - un[i][0];
-        float n1 = ((v21 * w1) + (2.0f * u1)) - un[i][1];
-        if (wsrc & (3u << (2 * i))) {
-          const int cell = gbase + i * NX;
+      for (int i = 0; i < S; ++i) {
+        if (i < nrows) {
+          const int z = zb + i;
+          const float2 A = lds2(Uc + i * NX - 2);
+          const float2 B = lds2(Uc + i * NX + 2);
+          float zm2[2], zm1[2], zp1[2], zp2[2];
+          if (i >= 2) {
+            zm2[0] = uc[i - 2][0];
+            zm2[1] = uc[i - 2][1];
+          } else {
+            const float2 q = lds2(Uc + (i - 2) * NX);
+            zm2[0] = q.x;
+            zm2[1] = q.y;
+          }
+          if (i >= 1) {
+            zm1[0] = uc[i - 1][0];
+            zm1[1] = uc[i - 1][1];
+          } else {
+            const float2 q = lds2(Uc + (i - 1) * NX);
+            zm1[0] = q.x;
+            zm1[1] = q.y;
+          }
+          if (i + 1 < S && (FULL || i + 1 < nrows)) {
+            zp1[0] = uc[i + 1 < S ? i + 1 : i][0];
+            zp1[1] = uc[i + 1 < S ? i + 1 : i][1];
+          } else {
+            const float2 q = lds2(Uc + (i + 1) * NX);
+            zp1[0] = q.x;
+            zp1[1] = q.y;
+          }
+          if (i + 2 < S && (FULL || i + 2 < nrows)) {
+            zp2[0] = uc[i + 2 < S ? i + 2 : i][0];
+            zp2[1] = uc[i + 2 < S ? i + 2 : i][1];
+          } else {
+            const float2 q = lds2(Uc + (i + 2) * NX);
+            zp2[0] = q.x;
+            zp2[1] = q.y;
+          }
+          const float u0 = uc[i][0], u1 = uc[i][1];
+          const float d2x0 = (((F_D2A * u0 + F_D2B * (u1 + A.y)) - F_D2C * (B.x + A.x)) * d2a) * d2b;
+          const float d2x1 = (((F_D2A * u1 + F_D2B * (B.x + u0)) - F_D2C * (B.y + A.y)) * d2a) * d2b;
+          float w0, w1;
+          if (pml) {
+            const float2 P0 = lds2(APXc + i * 2 * SW - 2);
+            const float2 P1 = lds2(APXc + i * 2 * SW);
+            const float2 P2 = lds2(APXc + i * 2 * SW + 2);
+            const float2 Z = lds2(zxo + i * 2 * SW);
+            const float d10 = ((F_D1A * (u1 - A.y)) - F_D1B * (B.x - A.x)) * rh;
+            const float d11 = ((F_D1A * (B.x - u0)) - F_D1B * (B.y - A.y)) * rh;
+            const float da0 = ((F_D1A * (P1.y - P0.y)) - F_D1B * (P2.x - P0.x)) * rh;
+            const float da1 = ((F_D1A * (P2.x - P1.x)) - F_D1B * (P2.y - P0.y)) * rh;
+            const float tmp0 = ((opbx0 * d2x0) + (dbx0 * d10)) + da0;
+            const float tmp1 = ((opbx1 * d2x1) + (dbx1 * d11)) + da1;
+            w0 = (opbx0 * tmp0) + (ax0 * Z.x);
+            w1 = (opbx1 * tmp1) + (ax1 * Z.y);
+            const float psi0 = (bx0 * d10) + P1.x;
+            const float psi1 = (bx1 * d11) + P1.y;
+            sts2(zxo + i * 2 * SW, (bx0 * tmp0) + (ax0 * Z.x), (bx1 * tmp1) + (ax1 * Z.y));
+            sts2(apxn + i * 2 * SW, ax0 * psi0, ax1 * psi1);
+          } else {
+            w0 = d2x0;
+            w1 = d2x1;
+          }
+          const float d2z0 = (((F_D2A * u0 + F_D2B * (zp1[0] + zm1[0])) - F_D2C * (zp2[0] + zm2[0])) * d2a) * d2b;
+          const float d2z1 = (((F_D2A * u1 + F_D2B * (zp1[1] + zm1[1])) - F_D2C * (zp2[1] + zm2[1])) * d2a) * d2b;
+          if (z < region || z >= nz - region) {
+            const float az = sAZ[z], bz = sBZ[z], dbz = sDBZ[z];
+            const float opbz = 1.0f + bz;
+            const float2 Qm2 = lds2(APZc + (i - 2) * NX);
+            const float2 Qm1 = lds2(APZc + (i - 1) * NX);
+            const float2 Q0 = lds2(APZc + i * NX);
+            const float2 Qp1 = lds2(APZc + (i + 1) * NX);
+            const float2 Qp2 = lds2(APZc + (i + 2) * NX);
+            const float2 Z = lds2(zzo + i * NX);
+            const float d10 = ((F_D1A * (zp1[0] - zm1[0])) - F_D1B * (zp2[0] - zm2[0])) * rh;
+            const float d11 = ((F_D1A * (zp1[1] - zm1[1])) - F_D1B * (zp2[1] - zm2[1])) * rh;
+            const float da0 = ((F_D1A * (Qp1.x - Qm1.x)) - F_D1B * (Qp2.x - Qm2.x)) * rh;
+            const float da1 = ((F_D1A * (Qp1.y - Qm1.y)) - F_D1B * (Qp2.y - Qm2.y)) * rh;
+            const float tmp0 = ((opbz * d2z0) + (dbz * d10)) + da0;
+            const float tmp1 = ((opbz * d2z1) + (dbz * d11)) + da1;
+            w0 = w0 + ((opbz * tmp0) + (az * Z.x));
+            w1 = w1 + ((opbz * tmp1) + (az * Z.y));
+            const float psi0 = (bz * d10) + Q0.x;
+            const float psi1 = (bz * d11) + Q0.y;
+            sts2(zzo + i * NX, (bz * tmp0) + (az * Z.x), (bz * tmp1) + (az * Z.y));
+            sts2(apzn + i * NX, az * psi0, az * psi1);
+          } else {
+            w0 = w0 + d2z0;
+            w1 = w1 + d2z1;
+          }
+          const float2 vv = lds2(V2o + i * NX);
+          const float v20 = vv.x, v21 = vv.y;
+          if (STORE) {
+            const float2 cc = lds2(C2o + i * NX);
+            if constexpr (kLateStore) stv[kLateStore ? i : 0] = make_float2(cc.x * w0, cc.y * w1);
+            else *reinterpret_cast<float2*>(stg + i * NX) = make_float2(cc.x * w0, cc.y * w1);
+          }
+          float n0 = ((v20 * w0) + (2.0f * u0)) - un[i][0];
+          float n1 = ((v21 * w1) + (2.0f * u1)) - un[i][1];
+          if (wsrc & (3u << (2 * i))) {
+            const int cell = gbase + i * NX;
 #pragma unroll
-          for (int k = 0; k < 4; ++k) {
-            const int c = sSrcCell[k];
-            const float q = sSrcQ[k] * f;
-            const float a0 = n0 + q, a1 = n1 + q;
-            n0 = (cell == c) ? a0 : n0;
-            n1 = (cell + 1 == c) ? a1 : n1;
+            for (int k = 0; k < 4; ++k) {
+              const int c = sSrcCell[k];
+              const float q = sSrcQ[k] * f;
+              const float a0 = n0 + q, a1 = n1 + q;
+              n0 = (cell == c) ? a0 : n0;
+              n1 = (cell + 1 == c) ? a1 : n1;
+            }
+          }
+          un[i][0] = n0;
+          un[i][1] = n1;
+          sts2(uw + i * NX, n0, n1);
+          if constexpr (C > 1) {
+            if (rank > 0 && z < r0 + FD_PAD) st_peer_v2(U + (1 - par) * ustride + (z - pr_lo) * NX + x, rank - 1, n0, n1);
+            if (rank < C - 1 && z >= r1 - FD_PAD)
+              st_peer_v2(U + (1 - par) * ustride + (z - (r1 - FD_PAD)) * NX + x, rank + 1, n0, n1);
           }
         }
-        un[i][0] = n0;
-        un[i][1] = n1;
-        sts2(Un + i * NX, n0, n1);
-        if constexpr (C > 1) {
-          if (rank > 0 && z < r0 + FD_PAD) st_peer_v2(U + (1 - par) * ustride + (z - pr_lo) * NX + x, rank - 1, n0, n1);
-          if (rank < C - 1 && z >= r1 - FD_PAD)
-            st_peer_v2(U + (1 - par) * ustride + (z - (r1 - FD_PAD)) * NX + x, rank + 1, n0, n1);
-        }
       }
-    }
+    };
+    rows(Un, APXn, ZXo, APZn, ZZo, st);
     if (TRACES) {
       // receivers at time t, recorded after this thread's update by the threads with the least
       // work per step: nothing writes buffer `par` before this step's barrier
