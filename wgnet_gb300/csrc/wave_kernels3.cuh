@@ -52,6 +52,17 @@ __device__ __forceinline__ int warp_role(int warp) {
 
 constexpr bool kLateStore = false;
 
+// Wavelet ring in shared memory: the sample of step u (counted from the launch's first step, in
+// the launch's direction) sits at W[u % G3_WAV_STEPS]. The launch starts with the first
+// G3_WAV_STEPS samples; every G3_WAV_STEPS / 2 steps the threads `ltid` < G3_WAV_STEPS / 2 load the
+// half G3_WAV_STEPS / 2 .. G3_WAV_STEPS steps ahead, before that step's barrier (the slots they
+// overwrite were read in earlier steps). `time(u)` maps a step count to the wavelet index.
+template <class TimeOf>
+__device__ __forceinline__ void wavelet_ring_fill(float* W, const float* wav, int u0, int u1, int steps, int tid,
+                                                  int nthreads, TimeOf time) {
+  for (int u = u0 + tid; u < u1 && u < steps; u += nthreads) W[u % G3_WAV_STEPS] = wav[time(u)];
+}
+
 // Thread order for the per-step receiver work (trace recording, residual staging): it starts at a
 // segment away from the z strips and from the rows sent to the peer CTAs, whose warps have the
 // least to do per step.
@@ -79,16 +90,20 @@ __device__ __forceinline__ void st_peer_v2(const float* local_ptr, unsigned peer
 // ------------------------------------------------------------------------------------------------
 // Forward (splatForward.wgsl:48-121)
 // ------------------------------------------------------------------------------------------------
-// SQ: the grid is square (nz = NX), so nz and every shared-memory offset are compile-time constants;
-// FULL: besides, the rows split evenly into the segments (every segment has exactly S rows).
-template <int NX, int PMLP, int C, int S, int NSEG, int NI, bool SQ, bool TRACES, bool STORE>
+// Row layouts (LAY): LAY_RUNTIME, any nz; LAY_EVEN, the rows split evenly into the segments (every
+// segment has exactly S rows); LAY_SQUARE, a square grid (nz = NX), so nz and every shared-memory
+// offset are compile-time constants (and the rows split evenly when C S NSEG = NX - 4).
+enum : int { LAY_RUNTIME = 0, LAY_EVEN = 1, LAY_SQUARE = 2 };
+
+template <int NX, int PMLP, int C, int S, int NSEG, int NI, int LAY, bool TRACES, bool STORE>
 __global__ void __launch_bounds__(NSEG * 32 * (1 + NI), 1) fwd3_kernel(const __grid_constant__ FwdArgs p) {
   using CL = Cols3<NX, PMLP>;
   constexpr int SW = CL::SW;
   constexpr int NT = NSEG * 32 * (1 + NI);
   extern __shared__ __align__(16) float sm[];
   const Grid& g = p.g;
-  constexpr bool FULL = SQ && (NX - 2 * FD_PAD == C * S * NSEG);
+  constexpr bool SQ = LAY == LAY_SQUARE;
+  constexpr bool FULL = LAY == LAY_EVEN || (SQ && NX - 2 * FD_PAD == C * S * NSEG);
   const int nz = SQ ? NX : g.nz;
   const int sw = g.sw, region = g.region, nrec = p.st.nrec;
   const float rh = g.rh, dt2 = g.dt2, d2a = g.d2a, d2b = g.d2b;
@@ -160,18 +175,20 @@ __global__ void __launch_bounds__(NSEG * 32 * (1 + NI), 1) fwd3_kernel(const __g
   const int* sc = p.st.src_cell + 4 * shot;
   const float* vel = p.vel + static_cast<size_t>(model) * cells + gbase;
   // Source corners: cell and the step-invariant factor (-v^2 dt^2) w of the shader's
-  // (((-v^2 dt^2) w) f); the wavelet sample of the next step is staged in F[(t + 1) & 1] by one
-  // thread before each step's barrier, so the injection reads shared memory only.
+  // (((-v^2 dt^2) w) f); the wavelet samples come from a ring in shared memory, so the injection
+  // reads shared memory only.
   int* sSrcCell = reinterpret_cast<int*>(sm + L.off_src);
   float* sSrcQ = sm + L.off_src + 4;
-  float* sF = sm + L.off_src + 8;
+  float* sW = sm + L.off_src + 8;
+  const int wsteps = p.t1 - p.t0;
+  auto wtime = [&](int u) { return p.t0 + u; };
   if (tid < 4) {
     const int cell = sc[tid];
     const float v = p.vel[static_cast<size_t>(model) * cells + cell];
     sSrcCell[tid] = cell;
     sSrcQ[tid] = (-(v * v * dt2)) * p.st.src_w[4 * shot + tid];
   }
-  if (ltid == 0) sF[p.t0 & 1] = g.wavelet[p.t0];
+  wavelet_ring_fill(sW, g.wavelet, 0, G3_WAV_STEPS, wsteps, tid, NT, wtime);
   float* V2o = sm + L.off_v2 + (zb - r0) * NX + x;  // owner-only coefficient rows
   float* C2o = sm + L.off_c2 + (zb - r0) * NX + x;
 #pragma unroll
@@ -274,7 +291,7 @@ __global__ void __launch_bounds__(NSEG * 32 * (1 + NI), 1) fwd3_kernel(const __g
       }
     }
 
-    const float f = sF[t & 1];
+    const float f = sW[(t - p.t0) % G3_WAV_STEPS];
     float* st = STORE ? p.stored + (static_cast<size_t>(unit) * (p.t1 - p.t0) + (t - p.t0)) * cells + gbase : nullptr;
     float2 stv[STORE && kLateStore ? S : 1];
     // The row updates write only through these restrict-qualified pointers (disjoint arrays), so
@@ -417,7 +434,11 @@ __global__ void __launch_bounds__(NSEG * 32 * (1 + NI), 1) fwd3_kernel(const __g
         }
       }
     }
-    if (ltid == 0 && t + 1 < p.t1) sF[(t + 1) & 1] = g.wavelet[t + 1];
+    {
+      constexpr int H = G3_WAV_STEPS / 2;
+      const int u = t - p.t0;
+      if (u >= H && u % H == 0) wavelet_ring_fill(sW, g.wavelet, u + H, u + 2 * H, wsteps, ltid, H, wtime);
+    }
     if constexpr (C > 1) {
       if (pusher) fence_cluster();
       __syncthreads();
@@ -445,15 +466,16 @@ __global__ void __launch_bounds__(NSEG * 32 * (1 + NI), 1) fwd3_kernel(const __g
 // ------------------------------------------------------------------------------------------------
 // PREF: fetch the next step's stored gradient terms between the barrier's arrive and wait (2 S more
 // registers per thread) instead of loading each row's terms when the row is processed.
-template <int NX, int PMLP, int C, int S, int NSEG, int NI, bool SQ, bool PREF>
+template <int NX, int PMLP, int C, int S, int NSEG, int NI, int LAY, bool PREF>
 __global__ void __launch_bounds__(NSEG * 32 * (1 + NI), 1) adj3_kernel(const __grid_constant__ AdjArgs p) {
   using CL = Cols3<NX, PMLP>;
   constexpr int SW = CL::SW;
   constexpr int NT = NSEG * 32 * (1 + NI);
   extern __shared__ __align__(16) float sm[];
   const Grid& g = p.g;
-  constexpr bool FULL = SQ && (NX - 2 * FD_PAD == C * S * NSEG);  // every segment has S rows
-  const int nz = SQ ? NX : g.nz;                                  // compile-time for square grids
+  constexpr bool SQ = LAY == LAY_SQUARE;
+  constexpr bool FULL = LAY == LAY_EVEN || (SQ && NX - 2 * FD_PAD == C * S * NSEG);  // S rows per segment
+  const int nz = SQ ? NX : g.nz;                                                     // compile-time if square
   const int swa = g.swa, region = g.region_adj, nrec = p.st.nrec, nt = g.nt;
   const float rh = g.rh, dt2 = g.dt2;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -508,11 +530,11 @@ __global__ void __launch_bounds__(NSEG * 32 * (1 + NI), 1) adj3_kernel(const __g
   // ((((-2 v) dt^2) w) f) (left to right, so the product with f rounds identically).
   int* sSrcCell = reinterpret_cast<int*>(sm + L.off_src);
   float* sSrcF = sm + L.off_src + 4;
-  // wavelet samples of this launch's steps, F[t - t_lo], when they fit
-  float* sF = sm + L.off_src + 8;
-  const bool wstage = p.t_hi - p.t_lo <= G3_WAV_STEPS;
-  if (wstage)
-    for (int i = tid; i < p.t_hi - p.t_lo; i += NT) sF[i] = g.wavelet[p.t_lo + i];
+  // wavelet ring, counted from the launch's first (latest) step backwards
+  float* sW = sm + L.off_src + 8;
+  const int wsteps = p.t_hi - p.t_lo;
+  auto wtime = [&](int u) { return p.t_hi - 1 - u; };
+  wavelet_ring_fill(sW, g.wavelet, 0, G3_WAV_STEPS, wsteps, tid, NT, wtime);
   if (tid < 4) {
     const int cell = p.st.src_cell[4 * shot + tid];
     sSrcCell[tid] = cell;
@@ -705,7 +727,7 @@ __global__ void __launch_bounds__(NSEG * 32 * (1 + NI), 1) adj3_kernel(const __g
     const float* U1Xd = U1Xs;
     const float* TZd = TZs;
     const float* U1Zd = U1Zs;
-    const float f = wstage ? sF[t - p.t_lo] : __ldg(&g.wavelet[t]);
+    const float f = sW[(p.t_hi - 1 - t) % G3_WAV_STEPS];
     const float* res_t = p.residual + (static_cast<size_t>(unit) * nt + t) * nrec;
     const float* st_t = p.stored + (static_cast<size_t>(unit) * segn + (t - p.t_lo)) * cells + gbase;
 #pragma unroll
@@ -815,6 +837,9 @@ __global__ void __launch_bounds__(NSEG * 32 * (1 + NI), 1) adj3_kernel(const __g
       __syncthreads();  // every read of the single-buffered strip terms of step t is done
       derive_strips(1 - par);
       if (stage && ltid < ecnt) sP[((t - 1) & 1) * L.pcap + ltid] = sEW[ltid] * rnext;
+      constexpr int H = G3_WAV_STEPS / 2;
+      const int u = p.t_hi - 1 - t;
+      if (u >= H && u % H == 0) wavelet_ring_fill(sW, g.wavelet, u + H, u + 2 * H, wsteps, ltid, H, wtime);
     }
     if constexpr (C > 1) {
       if (pusher) fence_cluster();
@@ -869,33 +894,50 @@ __global__ void __launch_bounds__(NSEG * 32 * (1 + NI), 1) adj3_kernel(const __g
   }
 }
 
+// Every segment of every CTA has exactly S rows when the CTAs' rows split evenly into NSEG segments.
+template <int C, int S, int NSEG>
+inline bool g3_even(int nz) {
+  for (int r = 0; r < C; ++r)
+    if (split_row(nz, C, r + 1) - split_row(nz, C, r) != S * NSEG) return false;
+  return true;
+}
+
+// Layout a launch takes: with one interior warp per segment a square grid takes the compile-time
+// layout; with several, the compile-time layout makes the forward spill registers and run slower
+// (measured), so evenly split grids take LAY_EVEN.
+template <int NX, int C, int S, int NSEG, int NI>
+inline int g3_layout(int nz) {
+  if (NI == 1) return nz == NX ? LAY_SQUARE : LAY_RUNTIME;
+  return g3_even<C, S, NSEG>(nz) ? LAY_EVEN : LAY_RUNTIME;
+}
+
+template <int NX, int PMLP, int C, int S, int NSEG, int NI, int LAY>
+cudaError_t fwd3_launch(bool traces, bool store, const FwdArgs& a, size_t smem, cudaStream_t s) {
+  constexpr int NT = NSEG * 32 * (1 + NI);
+  if (traces && store)
+    return launch_cluster(fwd3_kernel<NX, PMLP, C, S, NSEG, NI, LAY, true, true>, C, NT, a.units, smem, s, a);
+  if (traces)
+    return launch_cluster(fwd3_kernel<NX, PMLP, C, S, NSEG, NI, LAY, true, false>, C, NT, a.units, smem, s, a);
+  if (store)
+    return launch_cluster(fwd3_kernel<NX, PMLP, C, S, NSEG, NI, LAY, false, true>, C, NT, a.units, smem, s, a);
+  return cudaErrorInvalidValue;
+}
+
 template <int NX, int PMLP, int C, int S, int NSEG, int NI>
 cudaError_t fwd3_dispatch_impl(bool traces, bool store, const FwdArgs& a, size_t smem, cudaStream_t s) {
-  constexpr int NT = NSEG * 32 * (1 + NI);
-  if (a.g.nz == NX) {  // square grid: the compile-time layout
-    if (traces && store)
-      return launch_cluster(fwd3_kernel<NX, PMLP, C, S, NSEG, NI, true, true, true>, C, NT, a.units, smem, s, a);
-    if (traces)
-      return launch_cluster(fwd3_kernel<NX, PMLP, C, S, NSEG, NI, true, true, false>, C, NT, a.units, smem, s, a);
-    if (store)
-      return launch_cluster(fwd3_kernel<NX, PMLP, C, S, NSEG, NI, true, false, true>, C, NT, a.units, smem, s, a);
-    return cudaErrorInvalidValue;
-  }
-  if (traces && store)
-    return launch_cluster(fwd3_kernel<NX, PMLP, C, S, NSEG, NI, false, true, true>, C, NT, a.units, smem, s, a);
-  if (traces)
-    return launch_cluster(fwd3_kernel<NX, PMLP, C, S, NSEG, NI, false, true, false>, C, NT, a.units, smem, s, a);
-  if (store)
-    return launch_cluster(fwd3_kernel<NX, PMLP, C, S, NSEG, NI, false, false, true>, C, NT, a.units, smem, s, a);
-  return cudaErrorInvalidValue;
+  constexpr int LAY_FAST = NI == 1 ? LAY_SQUARE : LAY_EVEN;
+  if (g3_layout<NX, C, S, NSEG, NI>(a.g.nz) == LAY_FAST)
+    return fwd3_launch<NX, PMLP, C, S, NSEG, NI, LAY_FAST>(traces, store, a, smem, s);
+  return fwd3_launch<NX, PMLP, C, S, NSEG, NI, LAY_RUNTIME>(traces, store, a, smem, s);
 }
 
 template <int NX, int PMLP, int C, int S, int NSEG, int NI, bool PREF>
 cudaError_t adj3_dispatch_impl(const AdjArgs& a, size_t smem, cudaStream_t s) {
   constexpr int NT = NSEG * 32 * (1 + NI);
-  if (a.g.nz == NX)
-    return launch_cluster(adj3_kernel<NX, PMLP, C, S, NSEG, NI, true, PREF>, C, NT, a.units, smem, s, a);
-  return launch_cluster(adj3_kernel<NX, PMLP, C, S, NSEG, NI, false, PREF>, C, NT, a.units, smem, s, a);
+  constexpr int LAY_FAST = NI == 1 ? LAY_SQUARE : LAY_EVEN;
+  if (g3_layout<NX, C, S, NSEG, NI>(a.g.nz) == LAY_FAST)
+    return launch_cluster(adj3_kernel<NX, PMLP, C, S, NSEG, NI, LAY_FAST, PREF>, C, NT, a.units, smem, s, a);
+  return launch_cluster(adj3_kernel<NX, PMLP, C, S, NSEG, NI, LAY_RUNTIME, PREF>, C, NT, a.units, smem, s, a);
 }
 
 // Adjoint launch: the prefetching variant when `pref` is set in the shape.

@@ -10,6 +10,9 @@ namespace wg {
 
 __host__ __device__ inline int g3_sw(int pmlp) { return 2 * pmlp + 4; }  // packed strip width per side
 
+// Wavelet samples kept in shared memory: a ring over the launch's steps, refilled half at a time.
+constexpr int G3_WAV_STEPS = 128;
+
 struct F3Layout {
   int maxrows, lr, zs;
   int off_u, off_apx, off_zx, off_apz, off_zz, off_v2, off_c2, off_prof, off_rec, off_src, total;
@@ -30,15 +33,13 @@ __host__ __device__ inline F3Layout f3_layout_rt(int NX, int pmlp, int nz, int s
   L.off_c2 = L.off_v2 + L.maxrows * NX;           // C2[maxrows][NX]         2 v dt^2 (owner only)
   L.off_prof = L.off_c2 + L.maxrows * NX;
   L.off_rec = L.off_prof + 3 * (NX + nz);
-  L.off_src = (L.off_rec + 9 * nrec + 3) & ~3;  // source corners: 4 cells (int), 4 factors, wavelet[2]
-  L.total = L.off_src + 12;
+  L.off_src = (L.off_rec + 9 * nrec + 3) & ~3;  // source corners: 4 cells (int), 4 factors, wavelet ring
+  L.total = L.off_src + 8 + G3_WAV_STEPS;
   return L;
 }
 
 // Receiver rows of one CTA whose entry offsets the adjoint keeps in shared memory.
 constexpr int G3_REC_ROWS = 4;
-// Longest adjoint launch (in steps) whose wavelet samples are kept in shared memory.
-constexpr int G3_WAV_STEPS = 128;
 
 struct A3Layout {
   int maxrows, lr, zs;
