@@ -50,8 +50,6 @@ __device__ __forceinline__ int warp_role(int warp) {
   return j;
 }
 
-constexpr bool kLateStore = false;
-
 // Wavelet ring in shared memory: the sample of step u (counted from the launch's first step, in
 // the launch's direction) sits at W[u % G3_WAV_STEPS]. The launch starts with the first
 // G3_WAV_STEPS samples; every G3_WAV_STEPS / 2 steps the threads `ltid` < G3_WAV_STEPS / 2 load the
@@ -293,7 +291,6 @@ __global__ void __launch_bounds__(NSEG * 32 * (1 + NI), 1) fwd3_kernel(const __g
 
     const float f = sW[(t - p.t0) % G3_WAV_STEPS];
     float* st = STORE ? p.stored + (static_cast<size_t>(unit) * (p.t1 - p.t0) + (t - p.t0)) * cells + gbase : nullptr;
-    float2 stv[STORE && kLateStore ? S : 1];
     // The row updates write only through these restrict-qualified pointers (disjoint arrays), so
     // the compiler may issue a row's loads ahead of the previous row's stores.
     auto rows = [&](float* __restrict__ uw, float* __restrict__ apxn, float* __restrict__ zxo,
@@ -391,10 +388,9 @@ __global__ void __launch_bounds__(NSEG * 32 * (1 + NI), 1) fwd3_kernel(const __g
           }
           const float2 vv = lds2(V2o + i * NX);
           const float v20 = vv.x, v21 = vv.y;
-          if (STORE) {
+          if (STORE) {  // written as the row is updated: holding them for after the barrier spilled registers
             const float2 cc = lds2(C2o + i * NX);
-            if constexpr (kLateStore) stv[kLateStore ? i : 0] = make_float2(cc.x * w0, cc.y * w1);
-            else *reinterpret_cast<float2*>(stg + i * NX) = make_float2(cc.x * w0, cc.y * w1);
+            *reinterpret_cast<float2*>(stg + i * NX) = make_float2(cc.x * w0, cc.y * w1);
           }
           float n0 = ((v20 * w0) + (2.0f * u0)) - un[i][0];
           float n1 = ((v21 * w1) + (2.0f * u1)) - un[i][1];
@@ -443,11 +439,6 @@ __global__ void __launch_bounds__(NSEG * 32 * (1 + NI), 1) fwd3_kernel(const __g
       if (pusher) fence_cluster();
       __syncthreads();
       cluster_arrive_relaxed();
-    }
-    if constexpr (STORE && kLateStore) {  // the gradient terms go to global memory while the peers catch up
-#pragma unroll
-      for (int i = 0; i < S; ++i)
-        if (i < nrows) *reinterpret_cast<float2*>(st + i * NX) = stv[kLateStore ? i : 0];
     }
     if constexpr (C > 1) cluster_wait_acquire();
     else __syncthreads();
