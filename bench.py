@@ -45,7 +45,7 @@ UPDATED_CELLS = (NX + 2 * (PML + 2) - 4) ** 2  # 110 x 110 cells updated per ste
 FLOPS_PER_CELL_UPDATE = 48.0  # average over interior / one-PML-axis / two-PML-axes cells at pml 20
 # DRAM bytes per (unit, step) measured with ncu on the small case (32 models, nt 200) and scaled by
 # unit-steps to a full launch: profiles/adj3_kernel_b32_nt200.md, fwd3_kernel_recompute_b32_nt200.md
-MEASURED_TRAFFIC_PER_UNIT_STEP = {"adjoint": 445.93e6 / 8000 + 9.22e6 / 8000, "recompute": (65.0e6 + 341.1e6) / 8000}
+MEASURED_TRAFFIC_PER_UNIT_STEP = {"adjoint": (813.22e6 + 9.68e6) / 16000, "recompute": (69.83e6 + 736.70e6) / 16000}
 
 
 def clocks_sampler(stop: threading.Event, out: list):
