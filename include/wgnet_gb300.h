@@ -79,6 +79,13 @@ int wg_evaluate_adjoint(wg_engine* eng, const float* vel_mps, const float* obser
 int wg_evaluate_adjoint_dev(wg_engine* eng, const float* d_vel_mps, const float* d_observed, int models,
                             double* d_loss, float* d_grad, void* stream);
 
+/* Device status of the engine's last device-pointer call (wg_simulate_dev,
+ * wg_evaluate_adjoint_dev, wg_evaluate_adjoint_noalloc), which clear it when they start: waits for
+ * `stream`, then returns WG_OK, WG_ERR_ENERGY (observed traces with zero energy: the reference's
+ * `assert!(energy > 0)` panic, wave_wgpu.rs:853) or WG_ERR_CUDA (a kernel's bounded wait timed
+ * out), with the message in wg_last_error(). The host-pointer entry points check it themselves. */
+int wg_engine_status(wg_engine* eng, void* stream);
+
 /* Wavefield checkpoint interval for evaluate_adjoint: snapshots every k steps, segments recomputed
  * in reverse. k >= nt stores the gradient term of every step (the reference's scheme,
  * wave_wgpu.rs:181-182); so does k <= 0 on the resident path, while on the streamed path k <= 0
@@ -214,10 +221,14 @@ int wg_profile_read(wg_engine* eng, double* ms, long long* launches, int kinds);
  * framework's caching allocator that reserved the device, a service with a fixed memory budget).
  * Same inputs and outputs as wg_evaluate_adjoint_dev (device pointers, caller's stream); all
  * intermediates live in one static 48 MiB device array that the library holds on every GPU that
- * loads it until the process exits. Sizes needing more scratch (about 35 MiB per 70x70 5-shot
- * model at nt = 1000) are rejected with WG_ERR_ARG. The first call on a device looks up the
- * array's address (make that call before any stream capture). Calls share the array: calls that
- * overlap on the GPU (other streams, other threads) race and corrupt each other's results. */
+ * loads it until the process exits. Sizes needing more scratch (33 MiB for one 70x70 5-shot
+ * model at nt = 1000 and checkpoint interval 50, so one such model per call) are rejected with
+ * WG_ERR_ARG; when the engine's interval does not fit, the interval with the smallest footprint
+ * is used (the gradient is the same). The first call on a device after an engine was created
+ * there looks up the array's address (make that call before any stream capture); creating an
+ * engine drops the cached address, so a cudaDeviceReset followed by a new engine is safe. Calls
+ * share the array: calls that overlap on the GPU (other streams, other threads) race and corrupt
+ * each other's results. Read the call's device status with wg_engine_status. */
 int wg_evaluate_adjoint_noalloc(wg_engine* eng, const float* d_vel_mps, const float* d_observed, int models,
                                 double* d_loss, float* d_grad, void* stream);
 

@@ -110,7 +110,15 @@ def make_metrics(render) -> None:
     target = torch.nn.functional.avg_pool2d(target[:, None], 5, stride=1, padding=2)[:, 0]
     pred = target + 0.1 * torch.randn(4, 70, 70, generator=gen)
     m = render.field_metrics(pred, target)
-    np.savez(HERE / "metrics.npz", pred=pred.numpy(), target=target.numpy(),
+    # The same formula in f64: the reference's float32 window cast to f64 for this call only, so
+    # that the fixture pins the metric itself and not float32 rounding (its variance terms cancel).
+    window = render._gaussian_window
+    render._gaussian_window = lambda *a, **k: window(*a, **k).double()
+    try:
+        ssim64 = render.ssim(pred.double(), target.double())
+    finally:
+        render._gaussian_window = window
+    np.savez(HERE / "metrics.npz", pred=pred.numpy(), target=target.numpy(), ssim64=ssim64.numpy(),
              **{k: v.numpy() for k, v in m.items()})
 
 
@@ -132,8 +140,9 @@ def make_refine(refine) -> None:
 
 
 def main() -> None:
-    ref_root = Path(sys.argv[1]) if len(sys.argv) > 1 else Path("/root/reference")
-    mods = load_reference(ref_root)
+    if len(sys.argv) != 2:
+        raise SystemExit("usage: python tests/golden/make_golden.py <path to the WGNet checkout>")
+    mods = load_reference(Path(sys.argv[1]))
     torch.manual_seed(0)
     make_render(mods["render"])
     make_physics(mods["physics"])

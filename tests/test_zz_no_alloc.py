@@ -53,10 +53,33 @@ def test_noalloc_matches_the_allocating_entry_point_on_consecutive_calls(cuda_li
     for start, obs in cases + cases[:1]:  # two different calls in a row, then the first again
         rc, loss, grad = _call_noalloc(eng, start, obs, 1)
         _lib.check(rc, "wg_evaluate_adjoint_noalloc")
-        torch.cuda.synchronize()
+        _lib.check(_lib.load().wg_engine_status(eng._h, torch.cuda.current_stream().cuda_stream), "status")
         ref_loss, ref_grad = eng.evaluate_adjoint_torch(start, obs)
         torch.cuda.synchronize()
         assert torch.isfinite(grad).all()
+        np.testing.assert_array_equal(grad.cpu().numpy(), ref_grad.cpu().numpy())
+        np.testing.assert_allclose(loss.cpu().numpy(), ref_loss.cpu().numpy(), rtol=1e-12, atol=0)
+
+
+def test_noalloc_interval_fallback_matches_store_every_step(cuda_lib):
+    """With the engine set to keep every step's gradient term (about 260 MB at this size), the
+    scratch array cannot hold the engine's scheme, so the call picks the checkpoint interval with
+    the smallest footprint (59 steps here, which does not divide nt = 1000). The gradient must still
+    equal the allocating entry point's store-every-step result bit for bit."""
+    import torch
+
+    from wgnet_gb300 import _lib
+
+    eng = _engine()
+    eng.checkpoint_every = 0
+    true = torch.tensor(layered_model(21), device="cuda")[None]
+    start = torch.tensor(layered_model(121), device="cuda")[None].contiguous()
+    obs = eng.simulate_torch(true).contiguous()
+    ref_loss, ref_grad = eng.evaluate_adjoint_torch(start, obs)
+    for _ in range(2):
+        rc, loss, grad = _call_noalloc(eng, start, obs, 1)
+        _lib.check(rc, "wg_evaluate_adjoint_noalloc")
+        _lib.check(_lib.load().wg_engine_status(eng._h, torch.cuda.current_stream().cuda_stream), "status")
         np.testing.assert_array_equal(grad.cpu().numpy(), ref_grad.cpu().numpy())
         np.testing.assert_allclose(loss.cpu().numpy(), ref_loss.cpu().numpy(), rtol=1e-12, atol=0)
 

@@ -128,6 +128,7 @@ long to_index(float v) {
 namespace wg {
 int report_error(int code, const char* msg) { return fail(code, msg); }
 void note_launch() { ++g_launches; }
+void noalloc_forget_device(int dev);  // noalloc.cu
 }  // namespace wg
 
 struct wg_engine {
@@ -345,6 +346,7 @@ int create_impl(const wg_config* c, bool cpu_d2, wg_engine** out) {
   if (cfg.shots > 1 << 20 || cfg.nrec > 4096) return fail(WG_ERR_ARG, "too many shots or receivers");
   int dev = 0;
   WG_CK(cudaGetDevice(&dev));
+  wg::noalloc_forget_device(dev);
   auto e = new wg_engine();
   e->cfg = cfg;
   e->device = dev;
@@ -769,6 +771,8 @@ int wg_simulate_dev(wg_engine* e, const float* d_vel, int models, float* d_trace
   if (!e) return fail(WG_ERR_ARG, "null engine");
   std::lock_guard<std::mutex> lk(e->mu);
   WG_CK(cudaSetDevice(e->device));
+  // each call starts with a clear status word; wg_engine_status reads what this call's kernels set
+  WG_CK(cudaMemsetAsync(e->d_status.p, 0, sizeof(int), pick_stream(e, stream)));
   return simulate_dev_impl(e, d_vel, models, d_traces, pick_stream(e, stream));
 }
 
@@ -794,7 +798,21 @@ int wg_evaluate_adjoint_dev(wg_engine* e, const float* d_vel, const float* d_obs
   if (!e) return fail(WG_ERR_ARG, "null engine");
   std::lock_guard<std::mutex> lk(e->mu);
   WG_CK(cudaSetDevice(e->device));
+  WG_CK(cudaMemsetAsync(e->d_status.p, 0, sizeof(int), pick_stream(e, stream)));
   return gradient_dev_impl(e, d_vel, d_obs, models, d_loss, d_grad, pick_stream(e, stream));
+}
+
+int wg_engine_status(wg_engine* e, void* stream) {
+  if (!e) return fail(WG_ERR_ARG, "null engine");
+  std::lock_guard<std::mutex> lk(e->mu);
+  WG_CK(cudaSetDevice(e->device));
+  cudaStream_t st = pick_stream(e, stream);
+  int s = 0;
+  WG_CK(cudaMemcpyAsync(&s, e->d_status.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+  WG_CK(cudaStreamSynchronize(st));
+  if (s == wg::ST_ENERGY) return fail(WG_ERR_ENERGY, "Observed traces have zero energy");
+  if (s != 0) return fail(WG_ERR_CUDA, "device status " + std::to_string(s) + " (a pipeline wait timed out)");
+  return WG_OK;
 }
 
 int wg_evaluate_adjoint(wg_engine* e, const float* vel, const float* obs, int models, double* loss, float* grad) {

@@ -38,6 +38,21 @@ void* g_addr[kMaxDevices] = {};
 
 size_t up(size_t b) { return (b + kAlign - 1) / kAlign * kAlign; }
 
+}  // namespace
+
+namespace wg {
+// Called when an engine is created on `dev`: drops the cached scratch address of that device, so
+// that after a cudaDeviceReset (which may reload the module and move the array) the next call
+// looks it up again instead of launching on a stale address.
+void noalloc_forget_device(int dev) {
+  if (dev < 0 || dev >= kMaxDevices) return;
+  std::lock_guard<std::mutex> lk(g_addr_mu);
+  g_addr[dev] = nullptr;
+}
+}  // namespace wg
+
+namespace {
+
 // Scratch address on the current device (fetched once per device).
 int scratch_address(int dev, void** out) {
   if (dev < 0 || dev >= kMaxDevices) return wg::report_error(WG_ERR_CUDA, "device index out of range");
@@ -143,6 +158,12 @@ extern "C" int wg_evaluate_adjoint_noalloc(wg_engine* eng, const float* d_vel_mp
   const size_t per_model = static_cast<size_t>(v.shots) * v.nt * v.nrec;
   const size_t cells = static_cast<size_t>(v.nx) * v.nz;
 
+  // The status word starts clear; the energy kernel (zero-energy observed data) and the kernels'
+  // bounded waits set it, and wg_engine_status reads it once the stream has finished this call.
+  {
+    const cudaError_t e = cudaMemsetAsync(v.d_status, 0, sizeof(int), st);
+    if (e != cudaSuccess) return wg::report_error(WG_ERR_CUDA, cudaGetErrorString(e));
+  }
   NA_LAUNCH(wg::launch_pad_velocity(d_vel_mps, models, v.nx_vis, v.nz_vis, v.pad, v.vmin, v.vmax, vpad, mask, st));
   NA_LAUNCH(wg::launch_energy(d_observed, models, per_model, energy, scale, v.d_status, st));
   wg::FwdArgs f{};
@@ -153,11 +174,29 @@ extern "C" int wg_evaluate_adjoint_noalloc(wg_engine* eng, const float* d_vel_mp
   f.t0 = 0;
   f.t1 = v.nt;
   f.traces = traces;
-  f.ck_out = slots > 0 ? ckpt : nullptr;
-  f.ck_every = k;
-  f.ck_slots = slots;
   f.status = v.d_status;
-  NA_LAUNCH(wg::launch_fwd(v.fshape, true, false, f, st));
+  if (slots == 0) {
+    // one segment: the first pass keeps every step's gradient term
+    f.stored = stored;
+    NA_LAUNCH(wg::launch_fwd(v.fshape, true, true, f, st));
+  } else {
+    // As the allocating entry point does: steps [0, (J-1) k] with receivers and checkpoints, then
+    // the last segment from its checkpoint with receivers and stored terms, so the reverse sweep
+    // starts without a recompute.
+    f.ck_out = ckpt;
+    f.ck_every = k;
+    f.ck_slots = slots;
+    f.t1 = (J - 1) * k + 1;
+    NA_LAUNCH(wg::launch_fwd(v.fshape, true, false, f, st));
+    wg::FwdArgs l = f;
+    l.t0 = (J - 1) * k;
+    l.t1 = v.nt;
+    l.ck_out = nullptr;
+    l.ck_in = ckpt;
+    l.ck_in_slot = J - 2;
+    l.stored = stored;
+    NA_LAUNCH(wg::launch_fwd(v.fshape, true, true, l, st));
+  }
   NA_LAUNCH(wg::launch_residual(traces, d_observed, scale, models, per_model, traces, d_loss, st));
   // The accumulator's frame cells are never written by the kernels; the array keeps the previous
   // call's contents, so clear it.
@@ -191,7 +230,8 @@ extern "C" int wg_evaluate_adjoint_noalloc(wg_engine* eng, const float* d_vel_mp
     r.ck_every = k;
     r.stored = stored;
     r.status = v.d_status;
-    NA_LAUNCH(wg::launch_fwd(v.fshape, false, true, r, st));
+    if (j < J - 1)  // the last segment's terms are already stored by the first pass
+      NA_LAUNCH(wg::launch_fwd(v.fshape, false, true, r, st));
     a.t_hi = t1;
     a.t_lo = t0;
     a.first = (j == J - 1) ? 1 : 0;

@@ -1,5 +1,5 @@
 """Survey constants and engine factory of the reference's data module (python/wgnet/data.py:20-33,
-347-350). The OpenFWI loader and on-disk wave cache of that module are not part of this package;
+190-193). The OpenFWI loader and on-disk wave cache of that module are not part of this package;
 the synthetic model families used for benchmarks and tests live in `wgnet_gb300.models_synth`."""
 
 from __future__ import annotations
@@ -24,6 +24,6 @@ def make_engine(shots: int = SHOTS, nt: int = NT) -> PyWaveEngine:
 
 
 def source_positions_m(shots: int = SHOTS) -> np.ndarray:
-    """`[shots]` source x positions in metres matching the engine's default layout (data.py:347-350)."""
+    """`[shots]` source x positions in metres matching the engine's default layout (data.py:190-193)."""
     xmax = (N - 1) * H
     return np.array([xmax / 2.0], np.float32) if shots == 1 else np.linspace(0.0, xmax, shots, dtype=np.float32)

@@ -160,16 +160,29 @@ class WaveEngine:
             raise TypeError(f"{name} must be float32")
         return t.contiguous()
 
-    def simulate_torch(self, vel_mps):
+    def status(self, what: str = "") -> None:
+        """Wait for the current torch stream and raise if the engine's last device call set an error
+        (zero-energy observed data -> RuntimeError, as the reference's panic; a timed-out kernel
+        wait -> RuntimeError)."""
+        check(self._lib.wg_engine_status(self._h, _torch_stream()), what)
+
+    def simulate_torch(self, vel_mps, check_status: bool = True):
+        """Synthetics of CUDA velocities on the current stream. `check_status` waits for the stream
+        and raises on a device error; False leaves the call asynchronous (read it later with
+        `status()`)."""
         import torch
 
         v = self._dev(vel_mps, "vel_mps").reshape(-1, self.cells_vis)
         out = torch.empty((v.shape[0], self.shots, self.nt, self.nrec), device=v.device, dtype=torch.float32)
         with torch.cuda.device(v.device):
             check(self._lib.wg_simulate_dev(self._h, ptr(v), v.shape[0], ptr(out), _torch_stream()), "simulate")
+            if check_status:
+                self.status("simulate")
         return out
 
-    def evaluate_adjoint_torch(self, vel_mps, observed):
+    def evaluate_adjoint_torch(self, vel_mps, observed, check_status: bool = True):
+        """Misfit and gradient of CUDA tensors on the current stream; `check_status` as in
+        `simulate_torch` (zero-energy observed data raise RuntimeError)."""
         import torch
 
         v = self._dev(vel_mps, "vel_mps").reshape(-1, self.cells_vis)
@@ -182,6 +195,8 @@ class WaveEngine:
         with torch.cuda.device(v.device):
             check(self._lib.wg_evaluate_adjoint_dev(self._h, ptr(v), ptr(obs), b, ptr(loss), ptr(grad),
                                                     _torch_stream()), "evaluate_adjoint")
+            if check_status:
+                self.status("evaluate_adjoint")
         return loss, grad
 
 

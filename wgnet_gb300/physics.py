@@ -57,7 +57,10 @@ class WavePhysics:
         self.full_wavelet = self.engine.wavelet().copy()
         self.kernel: np.ndarray | None = None
         self.fmax: float | None = None
-        self.dt = DT
+        # The reference designs the passband at its module DT because its engine is fixed to that
+        # step (physics.py:43, data.py:25); here the engine's own step sets the filter, so a 1 ms
+        # engine gets a kernel sampled at 1 ms and the -3 dB point stays at the stated frequency.
+        self.dt = float(getattr(self.wave, "dt", DT))
 
     @property
     def wave(self) -> WaveEngine:

@@ -4,8 +4,9 @@ hand-written CUDA kernels.
 Layout as in the reference: one slot per 2x2-pixel cell of the 70x70 grid (35x35 = 1225 slots),
 6 activated parameters per slot `(dx, dz, log_sx, log_sz, angle, amp)`, each slot drawn in the
 25x25 pixel window around its anchor. `render_residual` is differentiable through
-`torch.autograd` (the backward is the CUDA VJP kernel). Parameter activation/clamping and the
-metrics (MAE, RMSE, SSIM) are small torch expressions, as in the reference.
+`torch.autograd` (the backward is the CUDA VJP kernel). Parameter activation/clamping keep the
+reference's expressions (they define the parametrisation); the metrics (MAE, RMSE, SSIM) are
+written here as a separable-window SSIM.
 """
 
 from __future__ import annotations
@@ -37,6 +38,33 @@ def slot_anchors(device: torch.device | str = "cpu") -> torch.Tensor:
     i = torch.arange(SLOT_SIDE, device=device, dtype=torch.float32)
     gz, gx = torch.meshgrid(2.0 * i + 1.0, 2.0 * i + 1.0, indexing="ij")
     return torch.stack([gx.reshape(-1), gz.reshape(-1)], dim=-1)
+
+
+_WINDOWS: dict[str, tuple[torch.Tensor, torch.Tensor, torch.Tensor]] = {}
+
+
+def slot_windows(device: torch.device | str = "cpu") -> tuple[torch.Tensor, torch.Tensor, torch.Tensor]:
+    """The pixels each slot draws (render.py:44-61): `(flat [N_SLOTS, 625] int64, centres
+    [N_SLOTS, 625, 2] f32, valid [N_SLOTS, 625] f32)`. Slot s = 35 iz + ix sits on pixel
+    (2 iz, 2 ix); window entry k covers pixel (2 iz + k // 25 - 12, 2 ix + k % 25 - 12), whose centre
+    is at index + 0.5. Pixels outside the 70 x 70 grid get the spare index 4900 and valid 0.
+    The CUDA kernels derive the same windows arithmetically; these tables serve callers that
+    scatter per-window values themselves."""
+    key = str(device)
+    hit = _WINDOWS.get(key)
+    if hit is not None:
+        return hit
+    slot = torch.arange(N_SLOTS, device=device)
+    k = torch.arange(WIN_SIDE * WIN_SIDE, device=device)
+    rows = 2 * torch.div(slot, SLOT_SIDE, rounding_mode="floor")[:, None] + (
+        torch.div(k, WIN_SIDE, rounding_mode="floor") - WINDOW)[None, :]
+    cols = 2 * torch.remainder(slot, SLOT_SIDE)[:, None] + (torch.remainder(k, WIN_SIDE) - WINDOW)[None, :]
+    inside = (rows >= 0) & (rows < GRID) & (cols >= 0) & (cols < GRID)
+    flat = torch.where(inside, rows * GRID + cols, torch.full_like(rows, GRID * GRID))
+    centres = torch.stack([cols.to(torch.float32) + 0.5, rows.to(torch.float32) + 0.5], dim=-1)
+    out = (flat, centres, inside.to(torch.float32))
+    _WINDOWS[key] = out
+    return out
 
 
 def activate_gaussians(raw: torch.Tensor) -> torch.Tensor:
@@ -98,35 +126,52 @@ def render_residual(params: torch.Tensor) -> torch.Tensor:
     return out.to(device=params.device, dtype=params.dtype)
 
 
-def _gaussian_window(size: int = 11, sigma: float = 1.5, device="cpu") -> torch.Tensor:
-    x = torch.arange(size, device=device, dtype=torch.float32) - (size - 1) / 2.0
-    g = torch.exp(-0.5 * (x / sigma) ** 2)
-    g = g / g.sum()
-    return (g[:, None] * g[None, :]).view(1, 1, size, size)
+# SSIM constants (Wang et al. 2004): an 11-tap Gaussian window of standard deviation 1.5 pixels,
+# stabilisers (0.01 L)^2 and (0.03 L)^2 for a dynamic range L = 1 of the normalised fields.
+SSIM_TAPS = 11
+SSIM_SIGMA = 1.5
+SSIM_C1 = 0.01**2
+SSIM_C2 = 0.03**2
+
+
+def _ssim_taps(device, dtype) -> torch.Tensor:
+    """Normalised 1-D Gaussian; the 2-D SSIM window is its outer product with itself."""
+    r = torch.linspace(-(SSIM_TAPS // 2), SSIM_TAPS // 2, SSIM_TAPS, device=device, dtype=torch.float64)
+    g = torch.exp(-(r * r) / (2.0 * SSIM_SIGMA * SSIM_SIGMA))
+    return (g / g.sum()).to(dtype)
+
+
+def _local_means(stack: torch.Tensor, taps: torch.Tensor) -> torch.Tensor:
+    """Windowed means of every channel of `[B, C, H, W]` over the valid (unpadded) region, as two
+    1-D passes (rows, then columns) of one grouped convolution each."""
+    c = stack.shape[1]
+    kx = taps.view(1, 1, 1, -1).expand(c, 1, 1, SSIM_TAPS)
+    kz = taps.view(1, 1, -1, 1).expand(c, 1, SSIM_TAPS, 1)
+    return F.conv2d(F.conv2d(stack, kx, groups=c), kz, groups=c)
 
 
 def ssim(pred_km: torch.Tensor, target_km: torch.Tensor) -> torch.Tensor:
-    """Per-sample SSIM `[B]` on `(v - 1.5) / 3.0`, 11x11 Gaussian window (render.py:123-137)."""
-    scale = V_MAX_KM - V_MIN_KM
-    x = ((pred_km - V_MIN_KM) / scale).unsqueeze(1)
-    y = ((target_km - V_MIN_KM) / scale).unsqueeze(1)
-    w = _gaussian_window(device=pred_km.device).to(x.dtype)
-    c1, c2 = 0.01**2, 0.03**2
-    mu_x = F.conv2d(x, w)
-    mu_y = F.conv2d(y, w)
-    sxx = F.conv2d(x * x, w) - mu_x**2
-    syy = F.conv2d(y * y, w) - mu_y**2
-    sxy = F.conv2d(x * y, w) - mu_x * mu_y
-    num = (2 * mu_x * mu_y + c1) * (2 * sxy + c2)
-    den = (mu_x**2 + mu_y**2 + c1) * (sxx + syy + c2)
-    return (num / den).mean(dim=(1, 2, 3))
+    """Per-sample mean SSIM `[B]` of two velocity fields after the OpenFWI normalisation
+    (v - 1.5) / 3 km/s (render.py:123-137 defines the metric): the five local moments of the pair
+    come from one separable Gaussian filtering of the stacked channels (x, y, x^2, y^2, x y)."""
+    x = (pred_km - V_MIN_KM) / (V_MAX_KM - V_MIN_KM)
+    y = (target_km - V_MIN_KM) / (V_MAX_KM - V_MIN_KM)
+    moments = _local_means(torch.stack([x, y, x * x, y * y, x * y], dim=1), _ssim_taps(x.device, x.dtype))
+    mx, my, exx, eyy, exy = moments.unbind(dim=1)
+    mxy = mx * my
+    var_sum = (exx - mx * mx) + (eyy - my * my)
+    cov = exy - mxy
+    index = ((2.0 * mxy + SSIM_C1) * (2.0 * cov + SSIM_C2)) / ((mx * mx + my * my + SSIM_C1) * (var_sum + SSIM_C2))
+    return index.flatten(1).mean(dim=1)
 
 
 @torch.no_grad()
 def field_metrics(pred_km: torch.Tensor, target_km: torch.Tensor) -> dict[str, torch.Tensor]:
-    """Per-sample `[B]` MAE and RMSE in m/s, SSIM, OpenFWI-normalized MAE / MSE (render.py:140-152)."""
-    err = (pred_km - target_km) * 1000.0
-    mae = err.abs().mean(dim=(1, 2))
-    mse = err.square().mean(dim=(1, 2))
-    return {"mae_mps": mae, "rmse_mps": mse.sqrt(), "ssim": ssim(pred_km, target_km), "mae_norm": mae / 1500.0,
-            "mse_norm": mse / 1500.0**2}
+    """Per-sample `[B]` velocity errors (render.py:140-152 defines the set): mean absolute and root
+    mean square error in m/s, SSIM, and the OpenFWI-normalised MAE and MSE (errors in units of
+    1500 m/s)."""
+    err_mps = ((pred_km - target_km) * 1000.0).flatten(1)
+    mae = err_mps.abs().mean(dim=1)
+    mse = (err_mps * err_mps).mean(dim=1)
+    return {"mae_mps": mae, "rmse_mps": torch.sqrt(mse), "ssim": ssim(pred_km, target_km), "mae_norm": mae / 1500.0,
+            "mse_norm": mse / (1500.0 * 1500.0)}
