@@ -546,6 +546,9 @@ def main():
     ap.add_argument("--nt", type=int, default=NT, help="time steps (profiling runs use a short record)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-autotune", action="store_true", help="keep the engine's default launch shapes")
+    ap.add_argument("--arith", default="exact", choices=["exact", "fast"],
+                    help="exact: the reference's f32 operation order (bit-identical results); fast: fused, "
+                         "reassociated stencils (within the stated f32 tolerances)")
     ap.add_argument("--workload", default="gradient", choices=["gradient", "datagen", "large", "train"],
                     help="gradient: the 256-model misfit-gradient batch (default); datagen: batched generation; "
                          "large: the 800x300 40-shot survey on the streamed path")
@@ -584,6 +587,7 @@ def main():
     eng = WaveEngine(shots=SHOTS, nt=nt, dt=DT, peak_hz=15.0, pml=PML, vmin=1000.0, vmax=5000.0,
                      checkpoint_every=args.checkpoint)
     eng.set_sources(src)
+    eng.set_option("arith", 1 if args.arith == "fast" else 0)
     tuned = None
     if not args.no_autotune:
         from wgnet_gb300.autotune import tune
@@ -686,7 +690,8 @@ def main():
                    "shots": SHOTS, "nt": nt, "checkpoint_every": args.checkpoint,
                    "l2": "inputs larger than L2 (observed 358 MB, checkpoints ~10 GB per step)",
                    "launch_shape": {"forward": eng.launch_shape("forward"), "adjoint": eng.launch_shape("adjoint")},
-                   "autotuned": tuned is not None},
+                   "autotuned": tuned is not None,
+                   "arith": args.arith},
         "gcell_updates_per_s": cells_per_s / 1e9,
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": launches,

@@ -89,9 +89,14 @@ class _FakeEngine:
     nrec = 70
     nz_vis = nx_vis = 70
 
-    def __init__(self):
+    def __init__(self, arith: int = 0):
         self.shape = {"forward": (2, 704, 10), "adjoint": (2, 704, 10)}
         self.set_calls = []
+        self.arith = arith
+
+    def get_option(self, key):
+        assert key == "arith"
+        return self.arith
 
     def shape_candidates(self, which):
         return [(2, 704, 10), (2, 896, 8), (4, 448, 8)]
@@ -113,6 +118,8 @@ def test_autotuner_cache_roundtrip_and_hit(tmp_path, monkeypatch):
     key_f = autotune.cache_key("GB300-test|sm152", "forward", eng)
     key_a = autotune.cache_key("GB300-test|sm152", "adjoint", eng)
     assert key_f != key_a and "114x114" in key_f and "nrec70" in key_f
+    # the fast-arithmetic kernels exist for some shapes only: their timings are cached apart
+    assert autotune.cache_key("GB300-test|sm152", "forward", _FakeEngine(arith=1)) != key_f
     autotune.store_cache({key_f: {"shape": [2, 896, 8]}, key_a: {"shape": [4, 448, 8]}}, path)
     autotune.store_cache({"other": {"shape": [1, 1, 1]}}, path)  # merge, not overwrite
     data = json.loads(path.read_text())

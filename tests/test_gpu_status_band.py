@@ -46,11 +46,13 @@ def test_set_band_uses_the_engine_step(cuda_lib, fmax):
     np.testing.assert_array_equal(k, physics_np.lowpass_kernel(fmax, 1e-3))
     expect = np.convolve(full, k, mode="full")[: eng.nt].astype(np.float32)
     np.testing.assert_array_equal(eng.wavelet(), expect)
-    # the kernel's -3 dB point is at fmax for a 1 ms sampling
+    # The Gaussian's amplitude response is exp(-2 pi^2 sigma^2 f^2) with sigma^2 = ln 2 / (2 pi^2 fmax^2):
+    # gain 1/2 (power -6 dB, the "-3 dB" of physics.py:19 in its own words) at f = fmax, when the
+    # kernel is sampled at the engine's 1 ms step (at 0.5 ms taps on a 1 ms engine it fell at fmax / 2).
     freqs = np.fft.rfftfreq(8192, d=1e-3)
     gain = np.abs(np.fft.rfft(k.astype(np.float64), 8192))
-    f3 = float(np.interp(1.0 / np.sqrt(2.0), gain[::-1], freqs[::-1]))
-    assert abs(f3 - fmax) < 0.05 * fmax, f3
+    f_half = float(np.interp(0.5, gain[::-1], freqs[::-1]))
+    assert abs(f_half - fmax) < 0.02 * fmax, f_half
     ph.set_band(None)
     np.testing.assert_array_equal(eng.wavelet(), full)
 

@@ -34,9 +34,10 @@ def device_tag() -> str:
 
 
 def cache_key(device: str, which: str, eng) -> str:
-    """The timing of a shape depends on the padded grid, the stations and the shot count; nt only
-    scales it."""
-    return f"{device}|{which}|{eng.nx}x{eng.nz}|pml{eng.pml}|shots{eng.shots}|nrec{eng.nrec}"
+    """The timing of a shape depends on the padded grid, the stations, the shot count and the
+    arithmetic (fast kernels exist for some shapes only); nt only scales it."""
+    arith = eng.get_option("arith")
+    return f"{device}|{which}|{eng.nx}x{eng.nz}|pml{eng.pml}|shots{eng.shots}|nrec{eng.nrec}|arith{arith}"
 
 
 def load_cache(path: Path | None = None) -> dict:

@@ -145,6 +145,7 @@ struct wg_engine {
   wg::Shape fshape{0, 0, 0}, ashape{0, 0, 0};
   int ck_every = 50;
   int adj_prefetch = 1;
+  int fast = 0;      // 1: fast-arithmetic resident kernels (option "arith")
   int streamed = 0;  // 1: wavefields in HBM, one launch per step (grids beyond the resident kernels)
   cudaStream_t copy_stream = nullptr;  // host->device copy of observed data, overlapping the forward
   cudaEvent_t obs_ready = nullptr;
@@ -214,6 +215,7 @@ wg::EngineView view_of(const wg_engine* e) {
   v.ashape = e->ashape;
   v.d_status = e->d_status.as<int>();
   v.adj_prefetch = e->adj_prefetch;
+  v.fast = e->fast;
   return v;
 }
 
@@ -522,6 +524,7 @@ int simulate_dev_impl(wg_engine* e, const float* d_vis, int models, float* d_tra
     a.t1 = e->nt;
     a.traces = d_traces + static_cast<size_t>(m0) * e->shots * e->nt * e->nrec;
     a.status = e->d_status.as<int>();
+    a.fast = e->fast;
     WG_LAUNCH(timed(e, K_FWD, st, [&] { return wg::launch_fwd(e->fshape, true, false, a, st); }));
   }
   return WG_OK;
@@ -573,6 +576,7 @@ int gradient_dev_impl(wg_engine* e, const float* d_vis, const float* d_obs, int 
     f.t1 = e->nt;
     f.traces = e->w_traces.as<float>();
     f.status = e->d_status.as<int>();
+    f.fast = e->fast;
     if (store_all) {
       f.stored = e->w_stored.as<float>();
       WG_LAUNCH(timed(e, K_FWD, st, [&] { return wg::launch_fwd(e->fshape, true, true, f, st); }));
@@ -612,6 +616,7 @@ int gradient_dev_impl(wg_engine* e, const float* d_vis, const float* d_obs, int 
     a.gacc = e->w_gacc.as<float>();
     a.status = e->d_status.as<int>();
     a.prefetch = e->adj_prefetch;
+    a.fast = e->fast;
     if (store_all) {
       a.t_hi = e->nt;
       a.t_lo = 0;
@@ -633,6 +638,7 @@ int gradient_dev_impl(wg_engine* e, const float* d_vis, const float* d_obs, int 
         r.ck_every = k;
         r.stored = e->w_stored.as<float>();
         r.status = e->d_status.as<int>();
+        r.fast = e->fast;
         if (j < J - 1)  // the last segment's terms are already stored by the first pass
           WG_LAUNCH(timed(e, K_RECOMPUTE, st, [&] { return wg::launch_fwd(e->fshape, false, true, r, st); }));
         a.t_hi = t1;
@@ -868,6 +874,9 @@ int wg_set_option(wg_engine* e, const char* key, int value) {
     e->ck_every = value;
   } else if (k == "adjoint_prefetch") {
     e->adj_prefetch = value ? 1 : 0;
+  } else if (k == "arith") {
+    if (value != 0 && value != 1) return fail(WG_ERR_ARG, "arith must be 0 (reference order) or 1 (fast)");
+    e->fast = value;
   } else if (k == "streamed") {
     if (value) {
       std::string why;
@@ -889,6 +898,8 @@ int wg_get_option(const wg_engine* e, const char* key, int* value) {
     *value = e->ck_every;
   } else if (k == "adjoint_prefetch") {
     *value = e->adj_prefetch;
+  } else if (k == "arith") {
+    *value = e->fast;
   } else if (k == "streamed") {
     *value = e->streamed;
   } else {

@@ -139,6 +139,7 @@ int record(wg_gen_plan* p) {
       a.t1 = v.nt;
       a.traces = static_cast<float*>(g.traces.p);
       a.status = v.d_status;
+      a.fast = v.fast;
       GP_LAUNCH(wg::launch_fwd(v.fshape, true, false, a, g.stream));
       auto* out = static_cast<unsigned short*>(g.out) + static_cast<size_t>(m0) * v.shots * nt_out * v.nrec;
       GP_LAUNCH(wg::launch_decimate(static_cast<const float*>(g.traces.p), static_cast<const float*>(p->d_taps.p),

@@ -175,6 +175,7 @@ extern "C" int wg_evaluate_adjoint_noalloc(wg_engine* eng, const float* d_vel_mp
   f.t1 = v.nt;
   f.traces = traces;
   f.status = v.d_status;
+  f.fast = v.fast;
   if (slots == 0) {
     // one segment: the first pass keeps every step's gradient term
     f.stored = stored;
@@ -215,6 +216,7 @@ extern "C" int wg_evaluate_adjoint_noalloc(wg_engine* eng, const float* d_vel_mp
   a.gacc = gacc;
   a.status = v.d_status;
   a.prefetch = v.adj_prefetch;
+  a.fast = v.fast;
   for (int j = J - 1; j >= 0; --j) {
     const int t0 = j * k, t1 = std::min(t0 + k, v.nt);
     wg::FwdArgs r{};
@@ -230,6 +232,7 @@ extern "C" int wg_evaluate_adjoint_noalloc(wg_engine* eng, const float* d_vel_mp
     r.ck_every = k;
     r.stored = stored;
     r.status = v.d_status;
+    r.fast = v.fast;
     if (j < J - 1)  // the last segment's terms are already stored by the first pass
       NA_LAUNCH(wg::launch_fwd(v.fshape, false, true, r, st));
     a.t_hi = t1;

@@ -23,17 +23,24 @@
 namespace wg {
 
 // Column layout of a generation-3 kernel.
+//
+// The PML warp's left pairs sit on lanes [0, PMLP) and its right pairs on lanes [16, 16 + PMLP):
+// a 64-bit shared-memory access is served per half-warp, and with the right pairs starting at lane
+// PMLP both halves of the row ran into the same banks (the last left pair and the first right pair
+// of a 114-wide row, and the packed strips' left and right columns), replaying a wavefront on
+// every access of the PML warp. Each half-warp now reads one contiguous run of columns.
 template <int NX, int PMLP>
 struct Cols3 {
+  static_assert(PMLP <= 16, "the PML warp holds at most 16 column pairs per side");
   static constexpr int PCOLS = 2 * PMLP;          // PML columns per side, starting at x = 2
   static constexpr int SW = PCOLS + 4;            // packed strip width per side (reads reach x+3); = g3_sw
   static constexpr int IPAIRS = (NX - 4 - 2 * PCOLS) / 2;
   __device__ static int x_of(int wk, int lane) {
-    if (wk == 0) return lane < PMLP ? FD_PAD + 2 * lane : (NX - FD_PAD - PCOLS) + 2 * (lane - PMLP);
+    if (wk == 0) return lane < 16 ? FD_PAD + 2 * lane : (NX - FD_PAD - PCOLS) + 2 * (lane - 16);
     return FD_PAD + PCOLS + 2 * ((wk - 1) * 32 + lane);
   }
   __device__ static bool active(int wk, int lane) {
-    if (wk == 0) return lane < 2 * PMLP;
+    if (wk == 0) return (lane & 15) < PMLP;
     return (wk - 1) * 32 + lane < IPAIRS;
   }
   __host__ __device__ static int strip(int x) { return x < SW ? x : x - (NX - 2 * SW); }
@@ -71,6 +78,36 @@ __device__ __forceinline__ int light_tid(int tid, int rank) {
   return (tid - ls * SEGT + NT) % NT;
 }
 
+// Fast arithmetic (FA kernels): the reference's stencils with 1/h and 1/h^2 folded into the weights
+// and the products fused (fmaf rounds once). The same discrete operators as the reference's
+// operation order, rounded differently: results agree with the unfused kernels to f32 accuracy,
+// not bit for bit. Weights: k0 = -5/2 / h^2, k1 = 4/3 / h^2, k2 = -1/12 / h^2 (second difference),
+// e1 = 2/3 / h, e2 = -1/12 / h (first difference); the adjoint's stencils carry the same numbers.
+struct FastCoef {
+  float k0, k1, k2, k00, e1, e2;
+  __device__ __forceinline__ static FastCoef make(float rh) {
+    const float rh2 = rh * rh;
+    FastCoef c;
+    c.k0 = F_D2A * rh2;
+    c.k1 = F_D2B * rh2;
+    c.k2 = -F_D2C * rh2;
+    c.k00 = 2.0f * c.k0;
+    c.e1 = F_D1A * rh;
+    c.e2 = -F_D1B * rh;
+    return c;
+  }
+  // second difference along one axis from the centre value and the sums of the +-1 and +-2 neighbours
+  __device__ __forceinline__ float d2(float u, float s1, float s2) const { return fmaf(k2, s2, fmaf(k1, s1, k0 * u)); }
+  // acc + the second difference along one axis
+  __device__ __forceinline__ float d2acc(float acc, float u, float s1, float s2) const {
+    return fmaf(k2, s2, fmaf(k1, s1, fmaf(k0, u, acc)));
+  }
+  // both axes' second differences of a cell, s1 / s2 summed over its four neighbours at distance 1 / 2
+  __device__ __forceinline__ float lap(float u, float s1, float s2) const { return fmaf(k2, s2, fmaf(k1, s1, k00 * u)); }
+  // first difference from (u[+1] - u[-1]) and (u[+2] - u[-2])
+  __device__ __forceinline__ float d1(float dd1, float dd2) const { return fmaf(e2, dd2, e1 * dd1); }
+};
+
 __device__ __forceinline__ float2 lds2(const float* p) { return *reinterpret_cast<const float2*>(p); }
 __device__ __forceinline__ void sts2(float* p, float a, float b) { *reinterpret_cast<float2*>(p) = make_float2(a, b); }
 
@@ -93,7 +130,8 @@ __device__ __forceinline__ void st_peer_v2(const float* local_ptr, unsigned peer
 // offset are compile-time constants (and the rows split evenly when C S NSEG = NX - 4).
 enum : int { LAY_RUNTIME = 0, LAY_EVEN = 1, LAY_SQUARE = 2 };
 
-template <int NX, int PMLP, int C, int S, int NSEG, int NI, int LAY, bool TRACES, bool STORE>
+// FA: fast arithmetic (see FastCoef); otherwise the reference's operation order, unfused.
+template <int NX, int PMLP, int C, int S, int NSEG, int NI, int LAY, bool TRACES, bool STORE, bool FA = false>
 __global__ void __launch_bounds__(NSEG * 32 * (1 + NI), 1) fwd3_kernel(const __grid_constant__ FwdArgs p) {
   using CL = Cols3<NX, PMLP>;
   constexpr int SW = CL::SW;
@@ -105,6 +143,7 @@ __global__ void __launch_bounds__(NSEG * 32 * (1 + NI), 1) fwd3_kernel(const __g
   const int nz = SQ ? NX : g.nz;
   const int sw = g.sw, region = g.region, nrec = p.st.nrec;
   const float rh = g.rh, dt2 = g.dt2, d2a = g.d2a, d2b = g.d2b;
+  const FastCoef fc = FastCoef::make(rh);
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int seg = warp / (1 + NI), wk = warp_role<NI>(warp);
   const int rank = (C > 1) ? static_cast<int>(cluster_rank()) : 0;
@@ -335,65 +374,133 @@ __global__ void __launch_bounds__(NSEG * 32 * (1 + NI), 1) fwd3_kernel(const __g
             zp2[1] = q.y;
           }
           const float u0 = uc[i][0], u1 = uc[i][1];
-          const float d2x0 = (((F_D2A * u0 + F_D2B * (u1 + A.y)) - F_D2C * (B.x + A.x)) * d2a) * d2b;
-          const float d2x1 = (((F_D2A * u1 + F_D2B * (B.x + u0)) - F_D2C * (B.y + A.y)) * d2a) * d2b;
-          float w0, w1;
-          if (pml) {
-            const float2 P0 = lds2(APXc + i * 2 * SW - 2);
-            const float2 P1 = lds2(APXc + i * 2 * SW);
-            const float2 P2 = lds2(APXc + i * 2 * SW + 2);
-            const float2 Z = lds2(zxo + i * 2 * SW);
-            const float d10 = ((F_D1A * (u1 - A.y)) - F_D1B * (B.x - A.x)) * rh;
-            const float d11 = ((F_D1A * (B.x - u0)) - F_D1B * (B.y - A.y)) * rh;
-            const float da0 = ((F_D1A * (P1.y - P0.y)) - F_D1B * (P2.x - P0.x)) * rh;
-            const float da1 = ((F_D1A * (P2.x - P1.x)) - F_D1B * (P2.y - P0.y)) * rh;
-            const float tmp0 = ((opbx0 * d2x0) + (dbx0 * d10)) + da0;
-            const float tmp1 = ((opbx1 * d2x1) + (dbx1 * d11)) + da1;
-            w0 = (opbx0 * tmp0) + (ax0 * Z.x);
-            w1 = (opbx1 * tmp1) + (ax1 * Z.y);
-            const float psi0 = (bx0 * d10) + P1.x;
-            const float psi1 = (bx1 * d11) + P1.y;
-            sts2(zxo + i * 2 * SW, (bx0 * tmp0) + (ax0 * Z.x), (bx1 * tmp1) + (ax1 * Z.y));
-            sts2(apxn + i * 2 * SW, ax0 * psi0, ax1 * psi1);
+          float n0, n1;
+          if constexpr (FA) {
+            // the same update, reassociated: 1/h and 1/h^2 folded into the stencil weights, the
+            // interior x and z second differences summed before weighting, products fused
+            const bool zpml = z < region || z >= nz - region;
+            float w0, w1;
+            if (pml) {
+              const float2 P0 = lds2(APXc + i * 2 * SW - 2);
+              const float2 P1 = lds2(APXc + i * 2 * SW);
+              const float2 P2 = lds2(APXc + i * 2 * SW + 2);
+              const float2 Z = lds2(zxo + i * 2 * SW);
+              // cell x: neighbours x-2..x+2 = A.x, A.y, u0, u1, B.x; cell x+1: A.y, u0, u1, B.x, B.y
+              const float d2x0 = fc.d2(u0, u1 + A.y, B.x + A.x);
+              const float d2x1 = fc.d2(u1, B.x + u0, B.y + A.y);
+              const float d10 = fc.d1(u1 - A.y, B.x - A.x);
+              const float d11 = fc.d1(B.x - u0, B.y - A.y);
+              const float da0 = fc.d1(P1.y - P0.y, P2.x - P0.x);
+              const float da1 = fc.d1(P2.x - P1.x, P2.y - P0.y);
+              const float tmp0 = fmaf(opbx0, d2x0, fmaf(dbx0, d10, da0));
+              const float tmp1 = fmaf(opbx1, d2x1, fmaf(dbx1, d11, da1));
+              const float az0 = ax0 * Z.x, az1 = ax1 * Z.y;
+              w0 = fmaf(opbx0, tmp0, az0);
+              w1 = fmaf(opbx1, tmp1, az1);
+              sts2(zxo + i * 2 * SW, fmaf(bx0, tmp0, az0), fmaf(bx1, tmp1, az1));
+              sts2(apxn + i * 2 * SW, ax0 * fmaf(bx0, d10, P1.x), ax1 * fmaf(bx1, d11, P1.y));
+              if (!zpml) {
+                w0 = fc.d2acc(w0, u0, zp1[0] + zm1[0], zp2[0] + zm2[0]);
+                w1 = fc.d2acc(w1, u1, zp1[1] + zm1[1], zp2[1] + zm2[1]);
+              }
+            } else if (!zpml) {  // interior in both axes: one weighted sum of both axes' neighbours
+              w0 = fc.lap(u0, (u1 + A.y) + (zp1[0] + zm1[0]), (B.x + A.x) + (zp2[0] + zm2[0]));
+              w1 = fc.lap(u1, (B.x + u0) + (zp1[1] + zm1[1]), (B.y + A.y) + (zp2[1] + zm2[1]));
+            } else {
+              w0 = fc.d2(u0, u1 + A.y, B.x + A.x);
+              w1 = fc.d2(u1, B.x + u0, B.y + A.y);
+            }
+            if (zpml) {
+              const float az = sAZ[z], bz = sBZ[z], dbz = sDBZ[z];
+              const float opbz = 1.0f + bz;
+              const float2 Qm2 = lds2(APZc + (i - 2) * NX);
+              const float2 Qm1 = lds2(APZc + (i - 1) * NX);
+              const float2 Q0 = lds2(APZc + i * NX);
+              const float2 Qp1 = lds2(APZc + (i + 1) * NX);
+              const float2 Qp2 = lds2(APZc + (i + 2) * NX);
+              const float2 Z = lds2(zzo + i * NX);
+              const float d2z0 = fc.d2(u0, zp1[0] + zm1[0], zp2[0] + zm2[0]);
+              const float d2z1 = fc.d2(u1, zp1[1] + zm1[1], zp2[1] + zm2[1]);
+              const float d10 = fc.d1(zp1[0] - zm1[0], zp2[0] - zm2[0]);
+              const float d11 = fc.d1(zp1[1] - zm1[1], zp2[1] - zm2[1]);
+              const float da0 = fc.d1(Qp1.x - Qm1.x, Qp2.x - Qm2.x);
+              const float da1 = fc.d1(Qp1.y - Qm1.y, Qp2.y - Qm2.y);
+              const float tmp0 = fmaf(opbz, d2z0, fmaf(dbz, d10, da0));
+              const float tmp1 = fmaf(opbz, d2z1, fmaf(dbz, d11, da1));
+              const float az0 = az * Z.x, az1 = az * Z.y;
+              w0 = w0 + fmaf(opbz, tmp0, az0);
+              w1 = w1 + fmaf(opbz, tmp1, az1);
+              sts2(zzo + i * NX, fmaf(bz, tmp0, az0), fmaf(bz, tmp1, az1));
+              sts2(apzn + i * NX, az * fmaf(bz, d10, Q0.x), az * fmaf(bz, d11, Q0.y));
+            }
+            const float2 vv = lds2(V2o + i * NX);
+            if (STORE) {
+              const float2 cc = lds2(C2o + i * NX);
+              *reinterpret_cast<float2*>(stg + i * NX) = make_float2(cc.x * w0, cc.y * w1);
+            }
+            n0 = fmaf(vv.x, w0, fmaf(2.0f, u0, -un[i][0]));
+            n1 = fmaf(vv.y, w1, fmaf(2.0f, u1, -un[i][1]));
           } else {
-            w0 = d2x0;
-            w1 = d2x1;
+            const float d2x0 = (((F_D2A * u0 + F_D2B * (u1 + A.y)) - F_D2C * (B.x + A.x)) * d2a) * d2b;
+            const float d2x1 = (((F_D2A * u1 + F_D2B * (B.x + u0)) - F_D2C * (B.y + A.y)) * d2a) * d2b;
+            float w0, w1;
+            if (pml) {
+              const float2 P0 = lds2(APXc + i * 2 * SW - 2);
+              const float2 P1 = lds2(APXc + i * 2 * SW);
+              const float2 P2 = lds2(APXc + i * 2 * SW + 2);
+              const float2 Z = lds2(zxo + i * 2 * SW);
+              const float d10 = ((F_D1A * (u1 - A.y)) - F_D1B * (B.x - A.x)) * rh;
+              const float d11 = ((F_D1A * (B.x - u0)) - F_D1B * (B.y - A.y)) * rh;
+              const float da0 = ((F_D1A * (P1.y - P0.y)) - F_D1B * (P2.x - P0.x)) * rh;
+              const float da1 = ((F_D1A * (P2.x - P1.x)) - F_D1B * (P2.y - P0.y)) * rh;
+              const float tmp0 = ((opbx0 * d2x0) + (dbx0 * d10)) + da0;
+              const float tmp1 = ((opbx1 * d2x1) + (dbx1 * d11)) + da1;
+              w0 = (opbx0 * tmp0) + (ax0 * Z.x);
+              w1 = (opbx1 * tmp1) + (ax1 * Z.y);
+              const float psi0 = (bx0 * d10) + P1.x;
+              const float psi1 = (bx1 * d11) + P1.y;
+              sts2(zxo + i * 2 * SW, (bx0 * tmp0) + (ax0 * Z.x), (bx1 * tmp1) + (ax1 * Z.y));
+              sts2(apxn + i * 2 * SW, ax0 * psi0, ax1 * psi1);
+            } else {
+              w0 = d2x0;
+              w1 = d2x1;
+            }
+            const float d2z0 = (((F_D2A * u0 + F_D2B * (zp1[0] + zm1[0])) - F_D2C * (zp2[0] + zm2[0])) * d2a) * d2b;
+            const float d2z1 = (((F_D2A * u1 + F_D2B * (zp1[1] + zm1[1])) - F_D2C * (zp2[1] + zm2[1])) * d2a) * d2b;
+            if (z < region || z >= nz - region) {
+              const float az = sAZ[z], bz = sBZ[z], dbz = sDBZ[z];
+              const float opbz = 1.0f + bz;
+              const float2 Qm2 = lds2(APZc + (i - 2) * NX);
+              const float2 Qm1 = lds2(APZc + (i - 1) * NX);
+              const float2 Q0 = lds2(APZc + i * NX);
+              const float2 Qp1 = lds2(APZc + (i + 1) * NX);
+              const float2 Qp2 = lds2(APZc + (i + 2) * NX);
+              const float2 Z = lds2(zzo + i * NX);
+              const float d10 = ((F_D1A * (zp1[0] - zm1[0])) - F_D1B * (zp2[0] - zm2[0])) * rh;
+              const float d11 = ((F_D1A * (zp1[1] - zm1[1])) - F_D1B * (zp2[1] - zm2[1])) * rh;
+              const float da0 = ((F_D1A * (Qp1.x - Qm1.x)) - F_D1B * (Qp2.x - Qm2.x)) * rh;
+              const float da1 = ((F_D1A * (Qp1.y - Qm1.y)) - F_D1B * (Qp2.y - Qm2.y)) * rh;
+              const float tmp0 = ((opbz * d2z0) + (dbz * d10)) + da0;
+              const float tmp1 = ((opbz * d2z1) + (dbz * d11)) + da1;
+              w0 = w0 + ((opbz * tmp0) + (az * Z.x));
+              w1 = w1 + ((opbz * tmp1) + (az * Z.y));
+              const float psi0 = (bz * d10) + Q0.x;
+              const float psi1 = (bz * d11) + Q0.y;
+              sts2(zzo + i * NX, (bz * tmp0) + (az * Z.x), (bz * tmp1) + (az * Z.y));
+              sts2(apzn + i * NX, az * psi0, az * psi1);
+            } else {
+              w0 = w0 + d2z0;
+              w1 = w1 + d2z1;
+            }
+            const float2 vv = lds2(V2o + i * NX);
+            const float v20 = vv.x, v21 = vv.y;
+            if (STORE) {  // written as the row is updated: holding them for after the barrier spilled registers
+              const float2 cc = lds2(C2o + i * NX);
+              *reinterpret_cast<float2*>(stg + i * NX) = make_float2(cc.x * w0, cc.y * w1);
+            }
+            n0 = ((v20 * w0) + (2.0f * u0)) - un[i][0];
+            n1 = ((v21 * w1) + (2.0f * u1)) - un[i][1];
           }
-          const float d2z0 = (((F_D2A * u0 + F_D2B * (zp1[0] + zm1[0])) - F_D2C * (zp2[0] + zm2[0])) * d2a) * d2b;
-          const float d2z1 = (((F_D2A * u1 + F_D2B * (zp1[1] + zm1[1])) - F_D2C * (zp2[1] + zm2[1])) * d2a) * d2b;
-          if (z < region || z >= nz - region) {
-            const float az = sAZ[z], bz = sBZ[z], dbz = sDBZ[z];
-            const float opbz = 1.0f + bz;
-            const float2 Qm2 = lds2(APZc + (i - 2) * NX);
-            const float2 Qm1 = lds2(APZc + (i - 1) * NX);
-            const float2 Q0 = lds2(APZc + i * NX);
-            const float2 Qp1 = lds2(APZc + (i + 1) * NX);
-            const float2 Qp2 = lds2(APZc + (i + 2) * NX);
-            const float2 Z = lds2(zzo + i * NX);
-            const float d10 = ((F_D1A * (zp1[0] - zm1[0])) - F_D1B * (zp2[0] - zm2[0])) * rh;
-            const float d11 = ((F_D1A * (zp1[1] - zm1[1])) - F_D1B * (zp2[1] - zm2[1])) * rh;
-            const float da0 = ((F_D1A * (Qp1.x - Qm1.x)) - F_D1B * (Qp2.x - Qm2.x)) * rh;
-            const float da1 = ((F_D1A * (Qp1.y - Qm1.y)) - F_D1B * (Qp2.y - Qm2.y)) * rh;
-            const float tmp0 = ((opbz * d2z0) + (dbz * d10)) + da0;
-            const float tmp1 = ((opbz * d2z1) + (dbz * d11)) + da1;
-            w0 = w0 + ((opbz * tmp0) + (az * Z.x));
-            w1 = w1 + ((opbz * tmp1) + (az * Z.y));
-            const float psi0 = (bz * d10) + Q0.x;
-            const float psi1 = (bz * d11) + Q0.y;
-            sts2(zzo + i * NX, (bz * tmp0) + (az * Z.x), (bz * tmp1) + (az * Z.y));
-            sts2(apzn + i * NX, az * psi0, az * psi1);
-          } else {
-            w0 = w0 + d2z0;
-            w1 = w1 + d2z1;
-          }
-          const float2 vv = lds2(V2o + i * NX);
-          const float v20 = vv.x, v21 = vv.y;
-          if (STORE) {  // written as the row is updated: holding them for after the barrier spilled registers
-            const float2 cc = lds2(C2o + i * NX);
-            *reinterpret_cast<float2*>(stg + i * NX) = make_float2(cc.x * w0, cc.y * w1);
-          }
-          float n0 = ((v20 * w0) + (2.0f * u0)) - un[i][0];
-          float n1 = ((v21 * w1) + (2.0f * u1)) - un[i][1];
           if (wsrc & (3u << (2 * i))) {
             const int cell = gbase + i * NX;
 #pragma unroll
@@ -457,7 +564,7 @@ __global__ void __launch_bounds__(NSEG * 32 * (1 + NI), 1) fwd3_kernel(const __g
 // ------------------------------------------------------------------------------------------------
 // PREF: fetch the next step's stored gradient terms between the barrier's arrive and wait (2 S more
 // registers per thread) instead of loading each row's terms when the row is processed.
-template <int NX, int PMLP, int C, int S, int NSEG, int NI, int LAY, bool PREF>
+template <int NX, int PMLP, int C, int S, int NSEG, int NI, int LAY, bool PREF, bool FA = false>
 __global__ void __launch_bounds__(NSEG * 32 * (1 + NI), 1) adj3_kernel(const __grid_constant__ AdjArgs p) {
   using CL = Cols3<NX, PMLP>;
   constexpr int SW = CL::SW;
@@ -469,6 +576,7 @@ __global__ void __launch_bounds__(NSEG * 32 * (1 + NI), 1) adj3_kernel(const __g
   const int nz = SQ ? NX : g.nz;                                                     // compile-time if square
   const int swa = g.swa, region = g.region_adj, nrec = p.st.nrec, nt = g.nt;
   const float rh = g.rh, dt2 = g.dt2;
+  const FastCoef fc = FastCoef::make(rh);
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int seg = warp / (1 + NI), wk = warp_role<NI>(warp);
   const int rank = (C > 1) ? static_cast<int>(cluster_rank()) : 0;
@@ -672,20 +780,34 @@ __global__ void __launch_bounds__(NSEG * 32 * (1 + NI), 1) adj3_kernel(const __g
           if (xs) {
             const float2 Z = pml ? lds2(LZX + i * 2 * SW) : make_float2(0.f, 0.f);
             const float2 P = pml ? lds2(LPX + i * 2 * SW) : make_float2(0.f, 0.f);
-            const float T0 = (o.x * vs0) + (bx.x * Z.x);
-            const float T1 = (o.y * vs1) + (bx.y * Z.y);
-            sts2(TXb + i * 2 * SW, T0, T1);
-            sts2(U1Xb + i * 2 * SW, (db.x * T0) + (bx.x * P.x), (db.y * T1) + (bx.y * P.y));
+            if constexpr (FA) {
+              const float T0 = fmaf(o.x, vs0, bx.x * Z.x);
+              const float T1 = fmaf(o.y, vs1, bx.y * Z.y);
+              sts2(TXb + i * 2 * SW, T0, T1);
+              sts2(U1Xb + i * 2 * SW, fmaf(db.x, T0, bx.x * P.x), fmaf(db.y, T1, bx.y * P.y));
+            } else {
+              const float T0 = (o.x * vs0) + (bx.x * Z.x);
+              const float T1 = (o.y * vs1) + (bx.y * Z.y);
+              sts2(TXb + i * 2 * SW, T0, T1);
+              sts2(U1Xb + i * 2 * SW, (db.x * T0) + (bx.x * P.x), (db.y * T1) + (bx.y * P.y));
+            }
           }
           if (zstrip) {
             const float bz = sBZ[z], dbz = sDBZ[z];
             const float opbz = 1.0f + bz;
             const float2 Z = lds2(LZZ + i * NX);
             const float2 P = lds2(LPZ + i * NX);
-            const float T0 = (opbz * vs0) + (bz * Z.x);
-            const float T1 = (opbz * vs1) + (bz * Z.y);
-            sts2(TZb + i * NX, T0, T1);
-            sts2(U1Zb + i * NX, (dbz * T0) + (bz * P.x), (dbz * T1) + (bz * P.y));
+            if constexpr (FA) {
+              const float T0 = fmaf(opbz, vs0, bz * Z.x);
+              const float T1 = fmaf(opbz, vs1, bz * Z.y);
+              sts2(TZb + i * NX, T0, T1);
+              sts2(U1Zb + i * NX, fmaf(dbz, T0, bz * P.x), fmaf(dbz, T1, bz * P.y));
+            } else {
+              const float T0 = (opbz * vs0) + (bz * Z.x);
+              const float T1 = (opbz * vs1) + (bz * Z.y);
+              sts2(TZb + i * NX, T0, T1);
+              sts2(U1Zb + i * NX, (dbz * T0) + (bz * P.x), (dbz * T1) + (bz * P.y));
+            }
           }
         }
       }
@@ -726,64 +848,133 @@ __global__ void __launch_bounds__(NSEG * 32 * (1 + NI), 1) adj3_kernel(const __g
       if (i < nrows) {
         const int z = zb + i;
         const float2 Vb = lds2(VSd + i * NX);  // own v^2 dt^2 lambda
-        float w0, w1;
-        if (pml) {
-          const float2 Ta = lds2(TXd + i * 2 * SW - 2), Tb = lds2(TXd + i * 2 * SW), Tc = lds2(TXd + i * 2 * SW + 2);
-          const float2 Ua = lds2(U1Xd + i * 2 * SW - 2), Ub = lds2(U1Xd + i * 2 * SW),
-                       Uc = lds2(U1Xd + i * 2 * SW + 2);
-          const float2 Oa = lds2(sOPB + x - 2), Ob = lds2(sOPB + x), Oc = lds2(sOPB + x + 2);
-          const float q0 = Oa.x * Ta.x, q1 = Oa.y * Ta.y, q2 = Ob.x * Tb.x, q3 = Ob.y * Tb.y, q4 = Oc.x * Tc.x,
-                      q5 = Oc.y * Tc.y;
-          // cell x: neighbours x-2..x+2 = (Ta.x, Ta.y, Tb.x, Tb.y, Tc.x)
-          const float du0 = ((F_D1A * (Ub.y - Ua.y)) + (A_D1B * (Uc.x - Ua.x))) * rh;
-          const float dd0 = ((((F_D2A * q2) + (F_D2B * (q3 + q1))) + (A_D2C * (q4 + q0))) * rh) * rh;
-          const float dt0 = ((F_D1A * (Tb.y - Ta.y)) + (A_D1B * (Tc.x - Ta.x))) * rh;
-          // cell x+1: neighbours x-1..x+3 = (Ta.y, Tb.x, Tb.y, Tc.x, Tc.y)
-          const float du1 = ((F_D1A * (Uc.x - Ub.x)) + (A_D1B * (Uc.y - Ua.y))) * rh;
-          const float dd1 = ((((F_D2A * q3) + (F_D2B * (q4 + q2))) + (A_D2C * (q5 + q1))) * rh) * rh;
-          const float dt1 = ((F_D1A * (Tc.x - Tb.x)) + (A_D1B * (Tc.y - Ta.y))) * rh;
-          w0 = (-du0) + dd0;
-          w1 = (-du1) + dd1;
-          const float2 P = lds2(LPX + i * 2 * SW);
-          const float2 Z = lds2(LZX + i * 2 * SW);
-          const float2 a = lds2(sAX + x);
-          sts2(LPX + i * 2 * SW, ((-a.x) * dt0) + (a.x * P.x), ((-a.y) * dt1) + (a.y * P.y));
-          sts2(LZX + i * 2 * SW, (a.x * Vb.x) + (a.x * Z.x), (a.y * Vb.y) + (a.y * Z.y));
+        float n0, n1;
+        if constexpr (FA) {
+          const bool zpml = z < region || z >= nz - region;
+          // x part first (as the unfused kernel), so the neighbours' loads are issued early
+          float w0 = 0.f, w1 = 0.f, sx10 = 0.f, sx11 = 0.f, sx20 = 0.f, sx21 = 0.f;
+          if (pml) {
+            const float2 Ta = lds2(TXd + i * 2 * SW - 2), Tb = lds2(TXd + i * 2 * SW), Tc = lds2(TXd + i * 2 * SW + 2);
+            const float2 Ua = lds2(U1Xd + i * 2 * SW - 2), Ub = lds2(U1Xd + i * 2 * SW),
+                         Uc = lds2(U1Xd + i * 2 * SW + 2);
+            const float2 Oa = lds2(sOPB + x - 2), Ob = lds2(sOPB + x), Oc = lds2(sOPB + x + 2);
+            const float q0 = Oa.x * Ta.x, q1 = Oa.y * Ta.y, q2 = Ob.x * Tb.x, q3 = Ob.y * Tb.y, q4 = Oc.x * Tc.x,
+                        q5 = Oc.y * Tc.y;
+            // cell x: neighbours x-2..x+2 = (Ta.x, Ta.y, Tb.x, Tb.y, Tc.x); cell x+1: (Ta.y .. Tc.y)
+            w0 = fc.d2(q2, q3 + q1, q4 + q0) - fc.d1(Ub.y - Ua.y, Uc.x - Ua.x);
+            w1 = fc.d2(q3, q4 + q2, q5 + q1) - fc.d1(Uc.x - Ub.x, Uc.y - Ua.y);
+            const float dt0 = fc.d1(Tb.y - Ta.y, Tc.x - Ta.x);
+            const float dt1 = fc.d1(Tc.x - Tb.x, Tc.y - Ta.y);
+            const float2 P = lds2(LPX + i * 2 * SW);
+            const float2 Z = lds2(LZX + i * 2 * SW);
+            const float2 a = lds2(sAX + x);
+            sts2(LPX + i * 2 * SW, a.x * (P.x - dt0), a.y * (P.y - dt1));
+            sts2(LZX + i * 2 * SW, a.x * (Vb.x + Z.x), a.y * (Vb.y + Z.y));
+          } else {
+            const float2 Va = lds2(VSd + i * NX - 2), Vc = lds2(VSd + i * NX + 2);
+            sx10 = Vb.y + Va.y;
+            sx20 = Vc.x + Va.x;
+            sx11 = Vc.x + Vb.x;
+            sx21 = Vc.y + Va.y;
+          }
+          if (zpml) {
+            const float2 Tm2 = lds2(TZd + (i - 2) * NX), Tm1 = lds2(TZd + (i - 1) * NX), T0 = lds2(TZd + i * NX),
+                         Tp1 = lds2(TZd + (i + 1) * NX), Tp2 = lds2(TZd + (i + 2) * NX);
+            const float2 Um2 = lds2(U1Zd + (i - 2) * NX), Um1 = lds2(U1Zd + (i - 1) * NX),
+                         Up1 = lds2(U1Zd + (i + 1) * NX), Up2 = lds2(U1Zd + (i + 2) * NX);
+            const float om2 = 1.0f + sBZ[z - 2], om1 = 1.0f + sBZ[z - 1], o0 = 1.0f + sBZ[z], op1 = 1.0f + sBZ[z + 1],
+                        op2 = 1.0f + sBZ[z + 2];
+            const float wz0 = fc.d2(o0 * T0.x, fmaf(op1, Tp1.x, om1 * Tm1.x), fmaf(op2, Tp2.x, om2 * Tm2.x)) -
+                              fc.d1(Up1.x - Um1.x, Up2.x - Um2.x);
+            const float wz1 = fc.d2(o0 * T0.y, fmaf(op1, Tp1.y, om1 * Tm1.y), fmaf(op2, Tp2.y, om2 * Tm2.y)) -
+                              fc.d1(Up1.y - Um1.y, Up2.y - Um2.y);
+            const float dt0 = fc.d1(Tp1.x - Tm1.x, Tp2.x - Tm2.x);
+            const float dt1 = fc.d1(Tp1.y - Tm1.y, Tp2.y - Tm2.y);
+            const float az = sAZ[z];
+            const float2 P = lds2(LPZ + i * NX);
+            const float2 Z = lds2(LZZ + i * NX);
+            sts2(LPZ + i * NX, az * (P.x - dt0), az * (P.y - dt1));
+            sts2(LZZ + i * NX, az * (Vb.x + Z.x), az * (Vb.y + Z.y));
+            if (pml) {
+              w0 = w0 + wz0;
+              w1 = w1 + wz1;
+            } else {
+              w0 = fc.d2acc(wz0, Vb.x, sx10, sx20);
+              w1 = fc.d2acc(wz1, Vb.y, sx11, sx21);
+            }
+          } else {
+            const float2 Vm2 = lds2(VSd + (i - 2) * NX), Vm1 = lds2(VSd + (i - 1) * NX), Vp1 = lds2(VSd + (i + 1) * NX),
+                         Vp2 = lds2(VSd + (i + 2) * NX);
+            if (pml) {
+              w0 = fc.d2acc(w0, Vb.x, Vp1.x + Vm1.x, Vp2.x + Vm2.x);
+              w1 = fc.d2acc(w1, Vb.y, Vp1.y + Vm1.y, Vp2.y + Vm2.y);
+            } else {
+              w0 = fc.lap(Vb.x, sx10 + (Vp1.x + Vm1.x), sx20 + (Vp2.x + Vm2.x));
+              w1 = fc.lap(Vb.y, sx11 + (Vp1.y + Vm1.y), sx21 + (Vp2.y + Vm2.y));
+            }
+          }
+          n0 = fmaf(2.0f, lc[i][0], w0 - lp[i][0]);
+          n1 = fmaf(2.0f, lc[i][1], w1 - lp[i][1]);
         } else {
-          const float2 Va = lds2(VSd + i * NX - 2), Vc = lds2(VSd + i * NX + 2);
-          w0 = ((((F_D2A * Vb.x) + (F_D2B * (Vb.y + Va.y))) + (A_D2C * (Vc.x + Va.x))) * rh) * rh;
-          w1 = ((((F_D2A * Vb.y) + (F_D2B * (Vc.x + Vb.x))) + (A_D2C * (Vc.y + Va.y))) * rh) * rh;
+          float w0, w1;
+          if (pml) {
+            const float2 Ta = lds2(TXd + i * 2 * SW - 2), Tb = lds2(TXd + i * 2 * SW), Tc = lds2(TXd + i * 2 * SW + 2);
+            const float2 Ua = lds2(U1Xd + i * 2 * SW - 2), Ub = lds2(U1Xd + i * 2 * SW),
+                         Uc = lds2(U1Xd + i * 2 * SW + 2);
+            const float2 Oa = lds2(sOPB + x - 2), Ob = lds2(sOPB + x), Oc = lds2(sOPB + x + 2);
+            const float q0 = Oa.x * Ta.x, q1 = Oa.y * Ta.y, q2 = Ob.x * Tb.x, q3 = Ob.y * Tb.y, q4 = Oc.x * Tc.x,
+                        q5 = Oc.y * Tc.y;
+            // cell x: neighbours x-2..x+2 = (Ta.x, Ta.y, Tb.x, Tb.y, Tc.x)
+            const float du0 = ((F_D1A * (Ub.y - Ua.y)) + (A_D1B * (Uc.x - Ua.x))) * rh;
+            const float dd0 = ((((F_D2A * q2) + (F_D2B * (q3 + q1))) + (A_D2C * (q4 + q0))) * rh) * rh;
+            const float dt0 = ((F_D1A * (Tb.y - Ta.y)) + (A_D1B * (Tc.x - Ta.x))) * rh;
+            // cell x+1: neighbours x-1..x+3 = (Ta.y, Tb.x, Tb.y, Tc.x, Tc.y)
+            const float du1 = ((F_D1A * (Uc.x - Ub.x)) + (A_D1B * (Uc.y - Ua.y))) * rh;
+            const float dd1 = ((((F_D2A * q3) + (F_D2B * (q4 + q2))) + (A_D2C * (q5 + q1))) * rh) * rh;
+            const float dt1 = ((F_D1A * (Tc.x - Tb.x)) + (A_D1B * (Tc.y - Ta.y))) * rh;
+            w0 = (-du0) + dd0;
+            w1 = (-du1) + dd1;
+            const float2 P = lds2(LPX + i * 2 * SW);
+            const float2 Z = lds2(LZX + i * 2 * SW);
+            const float2 a = lds2(sAX + x);
+            sts2(LPX + i * 2 * SW, ((-a.x) * dt0) + (a.x * P.x), ((-a.y) * dt1) + (a.y * P.y));
+            sts2(LZX + i * 2 * SW, (a.x * Vb.x) + (a.x * Z.x), (a.y * Vb.y) + (a.y * Z.y));
+          } else {
+            const float2 Va = lds2(VSd + i * NX - 2), Vc = lds2(VSd + i * NX + 2);
+            w0 = ((((F_D2A * Vb.x) + (F_D2B * (Vb.y + Va.y))) + (A_D2C * (Vc.x + Va.x))) * rh) * rh;
+            w1 = ((((F_D2A * Vb.y) + (F_D2B * (Vc.x + Vb.x))) + (A_D2C * (Vc.y + Va.y))) * rh) * rh;
+          }
+          if (z < region || z >= nz - region) {
+            const float2 Tm2 = lds2(TZd + (i - 2) * NX), Tm1 = lds2(TZd + (i - 1) * NX), T0 = lds2(TZd + i * NX),
+                         Tp1 = lds2(TZd + (i + 1) * NX), Tp2 = lds2(TZd + (i + 2) * NX);
+            const float2 Um2 = lds2(U1Zd + (i - 2) * NX), Um1 = lds2(U1Zd + (i - 1) * NX),
+                         Up1 = lds2(U1Zd + (i + 1) * NX), Up2 = lds2(U1Zd + (i + 2) * NX);
+            const float om2 = 1.0f + sBZ[z - 2], om1 = 1.0f + sBZ[z - 1], o0 = 1.0f + sBZ[z], op1 = 1.0f + sBZ[z + 1],
+                        op2 = 1.0f + sBZ[z + 2];
+            const float du0 = ((F_D1A * (Up1.x - Um1.x)) + (A_D1B * (Up2.x - Um2.x))) * rh;
+            const float du1 = ((F_D1A * (Up1.y - Um1.y)) + (A_D1B * (Up2.y - Um2.y))) * rh;
+            const float dd0 = ((((F_D2A * (o0 * T0.x)) + (F_D2B * ((op1 * Tp1.x) + (om1 * Tm1.x)))) +
+                                (A_D2C * ((op2 * Tp2.x) + (om2 * Tm2.x)))) * rh) * rh;
+            const float dd1 = ((((F_D2A * (o0 * T0.y)) + (F_D2B * ((op1 * Tp1.y) + (om1 * Tm1.y)))) +
+                                (A_D2C * ((op2 * Tp2.y) + (om2 * Tm2.y)))) * rh) * rh;
+            const float dt0 = ((F_D1A * (Tp1.x - Tm1.x)) + (A_D1B * (Tp2.x - Tm2.x))) * rh;
+            const float dt1 = ((F_D1A * (Tp1.y - Tm1.y)) + (A_D1B * (Tp2.y - Tm2.y))) * rh;
+            w0 = w0 + ((-du0) + dd0);
+            w1 = w1 + ((-du1) + dd1);
+            const float az = sAZ[z];
+            const float2 P = lds2(LPZ + i * NX);
+            const float2 Z = lds2(LZZ + i * NX);
+            sts2(LPZ + i * NX, ((-az) * dt0) + (az * P.x), ((-az) * dt1) + (az * P.y));
+            sts2(LZZ + i * NX, (az * Vb.x) + (az * Z.x), (az * Vb.y) + (az * Z.y));
+          } else {
+            const float2 Vm2 = lds2(VSd + (i - 2) * NX), Vm1 = lds2(VSd + (i - 1) * NX), Vp1 = lds2(VSd + (i + 1) * NX),
+                         Vp2 = lds2(VSd + (i + 2) * NX);
+            w0 = w0 + ((((F_D2A * Vb.x) + (F_D2B * (Vp1.x + Vm1.x))) + (A_D2C * (Vp2.x + Vm2.x))) * rh) * rh;
+            w1 = w1 + ((((F_D2A * Vb.y) + (F_D2B * (Vp1.y + Vm1.y))) + (A_D2C * (Vp2.y + Vm2.y))) * rh) * rh;
+          }
+          n0 = (w0 + (2.0f * lc[i][0])) - lp[i][0];
+          n1 = (w1 + (2.0f * lc[i][1])) - lp[i][1];
         }
-        if (z < region || z >= nz - region) {
-          const float2 Tm2 = lds2(TZd + (i - 2) * NX), Tm1 = lds2(TZd + (i - 1) * NX), T0 = lds2(TZd + i * NX),
-                       Tp1 = lds2(TZd + (i + 1) * NX), Tp2 = lds2(TZd + (i + 2) * NX);
-          const float2 Um2 = lds2(U1Zd + (i - 2) * NX), Um1 = lds2(U1Zd + (i - 1) * NX),
-                       Up1 = lds2(U1Zd + (i + 1) * NX), Up2 = lds2(U1Zd + (i + 2) * NX);
-          const float om2 = 1.0f + sBZ[z - 2], om1 = 1.0f + sBZ[z - 1], o0 = 1.0f + sBZ[z], op1 = 1.0f + sBZ[z + 1],
-                      op2 = 1.0f + sBZ[z + 2];
-          const float du0 = ((F_D1A * (Up1.x - Um1.x)) + (A_D1B * (Up2.x - Um2.x))) * rh;
-          const float du1 = ((F_D1A * (Up1.y - Um1.y)) + (A_D1B * (Up2.y - Um2.y))) * rh;
-          const float dd0 = ((((F_D2A * (o0 * T0.x)) + (F_D2B * ((op1 * Tp1.x) + (om1 * Tm1.x)))) +
-                              (A_D2C * ((op2 * Tp2.x) + (om2 * Tm2.x)))) * rh) * rh;
-          const float dd1 = ((((F_D2A * (o0 * T0.y)) + (F_D2B * ((op1 * Tp1.y) + (om1 * Tm1.y)))) +
-                              (A_D2C * ((op2 * Tp2.y) + (om2 * Tm2.y)))) * rh) * rh;
-          const float dt0 = ((F_D1A * (Tp1.x - Tm1.x)) + (A_D1B * (Tp2.x - Tm2.x))) * rh;
-          const float dt1 = ((F_D1A * (Tp1.y - Tm1.y)) + (A_D1B * (Tp2.y - Tm2.y))) * rh;
-          w0 = w0 + ((-du0) + dd0);
-          w1 = w1 + ((-du1) + dd1);
-          const float az = sAZ[z];
-          const float2 P = lds2(LPZ + i * NX);
-          const float2 Z = lds2(LZZ + i * NX);
-          sts2(LPZ + i * NX, ((-az) * dt0) + (az * P.x), ((-az) * dt1) + (az * P.y));
-          sts2(LZZ + i * NX, (az * Vb.x) + (az * Z.x), (az * Vb.y) + (az * Z.y));
-        } else {
-          const float2 Vm2 = lds2(VSd + (i - 2) * NX), Vm1 = lds2(VSd + (i - 1) * NX), Vp1 = lds2(VSd + (i + 1) * NX),
-                       Vp2 = lds2(VSd + (i + 2) * NX);
-          w0 = w0 + ((((F_D2A * Vb.x) + (F_D2B * (Vp1.x + Vm1.x))) + (A_D2C * (Vp2.x + Vm2.x))) * rh) * rh;
-          w1 = w1 + ((((F_D2A * Vb.y) + (F_D2B * (Vp1.y + Vm1.y))) + (A_D2C * (Vp2.y + Vm2.y))) * rh) * rh;
-        }
-        float n0 = (w0 + (2.0f * lc[i][0])) - lp[i][0];
-        float n1 = (w1 + (2.0f * lc[i][1])) - lp[i][1];
         const float2 sv = PREF ? stv[PREF ? i : 0] : __ldcs(reinterpret_cast<const float2*>(st_t + i * NX));
         // the shader starts the per-step gradient at +0; starting from the product itself differs
         // only in the sign of an exact zero
@@ -818,7 +1009,10 @@ __global__ void __launch_bounds__(NSEG * 32 * (1 + NI), 1) adj3_kernel(const __g
         }
         {
           const float2 ga = lds2(GAo + i * NX);
-          sts2(GAo + i * NX, ga.x + g0, ga.y + g1);
+          if (FA && !(wsrc & (3u << (2 * i))))  // fused when the row holds no source
+            sts2(GAo + i * NX, fmaf(lc[i][0], sv.x, ga.x), fmaf(lc[i][1], sv.y, ga.y));
+          else
+            sts2(GAo + i * NX, ga.x + g0, ga.y + g1);
         }
         lp[i][0] = n0;
         lp[i][1] = n1;
@@ -902,40 +1096,41 @@ inline int g3_layout(int nz) {
   return g3_even<C, S, NSEG>(nz) ? LAY_EVEN : LAY_RUNTIME;
 }
 
-template <int NX, int PMLP, int C, int S, int NSEG, int NI, int LAY>
+template <int NX, int PMLP, int C, int S, int NSEG, int NI, int LAY, bool FA>
 cudaError_t fwd3_launch(bool traces, bool store, const FwdArgs& a, size_t smem, cudaStream_t s) {
   constexpr int NT = NSEG * 32 * (1 + NI);
   if (traces && store)
-    return launch_cluster(fwd3_kernel<NX, PMLP, C, S, NSEG, NI, LAY, true, true>, C, NT, a.units, smem, s, a);
+    return launch_cluster(fwd3_kernel<NX, PMLP, C, S, NSEG, NI, LAY, true, true, FA>, C, NT, a.units, smem, s, a);
   if (traces)
-    return launch_cluster(fwd3_kernel<NX, PMLP, C, S, NSEG, NI, LAY, true, false>, C, NT, a.units, smem, s, a);
+    return launch_cluster(fwd3_kernel<NX, PMLP, C, S, NSEG, NI, LAY, true, false, FA>, C, NT, a.units, smem, s, a);
   if (store)
-    return launch_cluster(fwd3_kernel<NX, PMLP, C, S, NSEG, NI, LAY, false, true>, C, NT, a.units, smem, s, a);
+    return launch_cluster(fwd3_kernel<NX, PMLP, C, S, NSEG, NI, LAY, false, true, FA>, C, NT, a.units, smem, s, a);
   return cudaErrorInvalidValue;
 }
 
-template <int NX, int PMLP, int C, int S, int NSEG, int NI>
+// FA: the fast-arithmetic kernels (instantiated in their own translation units).
+template <int NX, int PMLP, int C, int S, int NSEG, int NI, bool FA = false>
 cudaError_t fwd3_dispatch_impl(bool traces, bool store, const FwdArgs& a, size_t smem, cudaStream_t s) {
   constexpr int LAY_FAST = NI == 1 ? LAY_SQUARE : LAY_EVEN;
   if (g3_layout<NX, C, S, NSEG, NI>(a.g.nz) == LAY_FAST)
-    return fwd3_launch<NX, PMLP, C, S, NSEG, NI, LAY_FAST>(traces, store, a, smem, s);
-  return fwd3_launch<NX, PMLP, C, S, NSEG, NI, LAY_RUNTIME>(traces, store, a, smem, s);
+    return fwd3_launch<NX, PMLP, C, S, NSEG, NI, LAY_FAST, FA>(traces, store, a, smem, s);
+  return fwd3_launch<NX, PMLP, C, S, NSEG, NI, LAY_RUNTIME, FA>(traces, store, a, smem, s);
 }
 
-template <int NX, int PMLP, int C, int S, int NSEG, int NI, bool PREF>
+template <int NX, int PMLP, int C, int S, int NSEG, int NI, bool PREF, bool FA>
 cudaError_t adj3_dispatch_impl(const AdjArgs& a, size_t smem, cudaStream_t s) {
   constexpr int NT = NSEG * 32 * (1 + NI);
   constexpr int LAY_FAST = NI == 1 ? LAY_SQUARE : LAY_EVEN;
   if (g3_layout<NX, C, S, NSEG, NI>(a.g.nz) == LAY_FAST)
-    return launch_cluster(adj3_kernel<NX, PMLP, C, S, NSEG, NI, LAY_FAST, PREF>, C, NT, a.units, smem, s, a);
-  return launch_cluster(adj3_kernel<NX, PMLP, C, S, NSEG, NI, LAY_RUNTIME, PREF>, C, NT, a.units, smem, s, a);
+    return launch_cluster(adj3_kernel<NX, PMLP, C, S, NSEG, NI, LAY_FAST, PREF, FA>, C, NT, a.units, smem, s, a);
+  return launch_cluster(adj3_kernel<NX, PMLP, C, S, NSEG, NI, LAY_RUNTIME, PREF, FA>, C, NT, a.units, smem, s, a);
 }
 
 // Adjoint launch: the prefetching variant when `pref` is set in the shape.
-template <int NX, int PMLP, int C, int S, int NSEG, int NI>
+template <int NX, int PMLP, int C, int S, int NSEG, int NI, bool FA = false>
 cudaError_t adj3_dispatch_impl_pref(const AdjArgs& a, size_t smem, cudaStream_t s) {
-  if (a.prefetch) return adj3_dispatch_impl<NX, PMLP, C, S, NSEG, NI, true>(a, smem, s);
-  return adj3_dispatch_impl<NX, PMLP, C, S, NSEG, NI, false>(a, smem, s);
+  if (a.prefetch) return adj3_dispatch_impl<NX, PMLP, C, S, NSEG, NI, true, FA>(a, smem, s);
+  return adj3_dispatch_impl<NX, PMLP, C, S, NSEG, NI, false, FA>(a, smem, s);
 }
 
 }  // namespace wg

@@ -31,6 +31,11 @@ template <int NX, int PMLP, int C, int S, int NSEG, int NI>
 cudaError_t fwd3_dispatch(bool traces, bool store, const FwdArgs& a, size_t smem, cudaStream_t s);
 template <int NX, int PMLP, int C, int S, int NSEG, int NI>
 cudaError_t adj3_dispatch(const AdjArgs& a, size_t smem, cudaStream_t s);
+// fast-arithmetic variants, compiled for the shapes of WG_G3_FAST_SHAPES (wave_table.cu)
+template <int NX, int PMLP, int C, int S, int NSEG, int NI>
+cudaError_t fwd3f_dispatch(bool traces, bool store, const FwdArgs& a, size_t smem, cudaStream_t s);
+template <int NX, int PMLP, int C, int S, int NSEG, int NI>
+cudaError_t adj3f_dispatch(const AdjArgs& a, size_t smem, cudaStream_t s);
 
 // Forward over units = models * shots. traces: record receivers; store: write 2 v dt^2 w.
 cudaError_t launch_fwd(const Shape& s, bool traces, bool store, const FwdArgs& a, cudaStream_t stream);
@@ -80,6 +85,7 @@ struct EngineView {
   Shape fshape, ashape;
   int* d_status;
   int adj_prefetch;
+  int fast;  // fast-arithmetic kernels (engine option "arith")
 };
 
 // Event marks around groups of launches (kind 0 forward, 1 forward recompute, 2 adjoint) for the

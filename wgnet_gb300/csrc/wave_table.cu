@@ -31,6 +31,13 @@ namespace wg {
   X(184, 12, 6, 6, 5, 3)        \
   X(184, 12, 6, 10, 3, 3)
 
+// generation-3 shapes that also have fast-arithmetic kernels (one instantiation file each): the
+// default shape of each of the 70x70, 100x100 and 140x140 grids at pml 20
+#define WG_G3_FAST_SHAPES(X)    \
+  X(114, 12, 2, 5, 11, 1)       \
+  X(144, 12, 4, 5, 7, 2)        \
+  X(184, 12, 6, 6, 5, 3)
+
 #define WG_ADJ_SHAPES(X) \
   X(2, 1024, 6)          \
   X(2, 512, 12)          \
@@ -48,10 +55,26 @@ static const Shape kAdjShapes[] = {WG_G3_SHAPES(WG_LIST3) WG_ADJ_SHAPES(WG_LIST)
 #undef WG_LIST
 #undef WG_LIST3
 
+// Whether the fast-arithmetic kernels exist for a generation-3 shape.
+static bool g3_has_fast(const Shape& s) {
+#define WG_HASF(NXs, PMLPs, Cc, Ss, NSEGs, NIs)                                                                  \
+  if (s.kind == 3 && s.nxc == NXs && s.pmlp == PMLPs && s.cluster == Cc && s.seg_rows == Ss && s.nseg == NSEGs && \
+      s.ni == NIs)                                                                                                 \
+    return true;
+  WG_G3_FAST_SHAPES(WG_HASF)
+#undef WG_HASF
+  return false;
+}
+
+static Shape with_fast(Shape s) {
+  s.fast = g3_has_fast(s) ? 1 : 0;
+  return s;
+}
+
 int fwd_shape_count() { return static_cast<int>(sizeof(kFwdShapes) / sizeof(kFwdShapes[0])); }
 int adj_shape_count() { return static_cast<int>(sizeof(kAdjShapes) / sizeof(kAdjShapes[0])); }
-Shape fwd_shape(int i) { return kFwdShapes[i]; }
-Shape adj_shape(int i) { return kAdjShapes[i]; }
+Shape fwd_shape(int i) { return with_fast(kFwdShapes[i]); }
+Shape adj_shape(int i) { return with_fast(kAdjShapes[i]); }
 
 size_t fwd_smem_bytes(const Shape& s, int nx, int nz, int sw, int nrec) {
   if (s.kind == 3) return static_cast<size_t>(f3_layout_rt(s.nxc, s.pmlp, nz, sw, s.cluster, nrec).total) * sizeof(float);
@@ -108,6 +131,13 @@ bool adj_shape_fits(const Shape& s, int nx, int nz, int swa, int nrec) {
 cudaError_t launch_fwd(const Shape& s, bool traces, bool store, const FwdArgs& a, cudaStream_t stream) {
   const size_t smem = fwd_smem_bytes(s, a.g.nx, a.g.nz, a.g.sw, a.st.nrec);
   if (s.kind == 3) {
+    if (a.fast) {  // shapes without fast-arithmetic kernels run the unfused ones
+#define WG_FWD3F(NXs, PMLPs, Cc, Ss, NSEGs, NIs)                                                                 \
+  if (s.nxc == NXs && s.pmlp == PMLPs && s.cluster == Cc && s.seg_rows == Ss && s.nseg == NSEGs && s.ni == NIs) \
+    return fwd3f_dispatch<NXs, PMLPs, Cc, Ss, NSEGs, NIs>(traces, store, a, smem, stream);
+      WG_G3_FAST_SHAPES(WG_FWD3F)
+#undef WG_FWD3F
+    }
 #define WG_FWD3(NXs, PMLPs, Cc, Ss, NSEGs, NIs)                                                                  \
   if (s.nxc == NXs && s.pmlp == PMLPs && s.cluster == Cc && s.seg_rows == Ss && s.nseg == NSEGs && s.ni == NIs) \
     return fwd3_dispatch<NXs, PMLPs, Cc, Ss, NSEGs, NIs>(traces, store, a, smem, stream);
@@ -125,6 +155,13 @@ cudaError_t launch_fwd(const Shape& s, bool traces, bool store, const FwdArgs& a
 cudaError_t launch_adj(const Shape& s, const AdjArgs& a, cudaStream_t stream) {
   const size_t smem = adj_smem_bytes(s, a.g.nx, a.g.nz, a.g.swa, a.st.nrec);
   if (s.kind == 3) {
+    if (a.fast) {
+#define WG_ADJ3F(NXs, PMLPs, Cc, Ss, NSEGs, NIs)                                                                 \
+  if (s.nxc == NXs && s.pmlp == PMLPs && s.cluster == Cc && s.seg_rows == Ss && s.nseg == NSEGs && s.ni == NIs) \
+    return adj3f_dispatch<NXs, PMLPs, Cc, Ss, NSEGs, NIs>(a, smem, stream);
+      WG_G3_FAST_SHAPES(WG_ADJ3F)
+#undef WG_ADJ3F
+    }
 #define WG_ADJ3(NXs, PMLPs, Cc, Ss, NSEGs, NIs)                                                                  \
   if (s.nxc == NXs && s.pmlp == PMLPs && s.cluster == Cc && s.seg_rows == Ss && s.nseg == NSEGs && s.ni == NIs) \
     return adj3_dispatch<NXs, PMLPs, Cc, Ss, NSEGs, NIs>(a, smem, stream);
