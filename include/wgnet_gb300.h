@@ -99,10 +99,11 @@ int wg_get_checkpoint_interval(const wg_engine* eng);
  * (0/1: wavefields in device memory and one launch per time step instead of the resident
  * kernels; engines whose grid fits no resident kernel start with 1; needs a padded width
  * nx_vis + 2 (pml + 2) divisible by 4), "arith" (0, the default: every f32 operation in the
- * reference's order, unfused, so results equal the reference's bit for bit; 1: the same
- * discrete operators with 1/h folded into the stencil weights and fused multiply-adds, faster
- * and equal to f32 accuracy, on the resident kernels of the default 70x70, 100x100 and 140x140
- * shapes; other shapes and the streamed path run the unfused kernels). No reference counterpart. */
+ * reference's order, unfused, so results equal the reference's bit for bit; 1: the forward
+ * kernels compute the same discrete operator with 1/h folded into the stencil weights and fused
+ * multiply-adds, faster and equal to f32 accuracy, on the resident kernels of the default 70x70,
+ * 100x100 and 140x140 shapes; the adjoint, other shapes and the streamed path keep the unfused
+ * arithmetic). No reference counterpart. */
 int wg_set_option(wg_engine* eng, const char* key, int value);
 int wg_get_option(const wg_engine* eng, const char* key, int* value);
 

@@ -616,7 +616,6 @@ int gradient_dev_impl(wg_engine* e, const float* d_vis, const float* d_obs, int 
     a.gacc = e->w_gacc.as<float>();
     a.status = e->d_status.as<int>();
     a.prefetch = e->adj_prefetch;
-    a.fast = e->fast;
     if (store_all) {
       a.t_hi = e->nt;
       a.t_lo = 0;

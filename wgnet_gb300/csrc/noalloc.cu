@@ -216,7 +216,6 @@ extern "C" int wg_evaluate_adjoint_noalloc(wg_engine* eng, const float* d_vel_mp
   a.gacc = gacc;
   a.status = v.d_status;
   a.prefetch = v.adj_prefetch;
-  a.fast = v.fast;
   for (int j = J - 1; j >= 0; --j) {
     const int t0 = j * k, t1 = std::min(t0 + k, v.nt);
     wg::FwdArgs r{};

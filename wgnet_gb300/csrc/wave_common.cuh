@@ -99,7 +99,6 @@ struct AdjArgs {
   float* gacc;           // [units][nz][nx] gradient accumulator (per shot, padded grid)
   int* status;
   int prefetch;          // generation-3 adjoint: fetch the next step's stored terms a step ahead
-  int fast;              // 1: fast-arithmetic kernels where the shape has them (fused, reassociated)
 };
 
 // Status codes shared with the C ABI (include/wgnet_gb300.h defines the same numbers).
@@ -122,7 +121,7 @@ struct Shape {
   int cluster, threads, cpt;
   int kind = 1, seg_rows = 0, nseg = 0, ni = 0;
   int nxc = 0, pmlp = 0;  // generation 3: compile-time grid width and PML column pairs per side
-  int fast = 0;           // generation 3: fast-arithmetic kernels compiled for this shape
+  int fast = 0;           // generation 3: fast-arithmetic forward compiled for this shape
 };
 
 }  // namespace wg

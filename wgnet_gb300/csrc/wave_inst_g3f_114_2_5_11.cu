@@ -1,4 +1,4 @@
-// Explicit instantiation of the generation-3 fast-arithmetic kernels for one launch shape (see
+// Explicit instantiation of the generation-3 fast-arithmetic forward kernels for one launch shape (see
 // wave_table.cu).
 #include "wave_kernels3.cuh"
 
@@ -7,11 +7,6 @@ namespace wg {
 template <>
 cudaError_t fwd3f_dispatch<114, 12, 2, 5, 11, 1>(bool traces, bool store, const FwdArgs& a, size_t smem, cudaStream_t s) {
   return fwd3_dispatch_impl<114, 12, 2, 5, 11, 1, true>(traces, store, a, smem, s);
-}
-
-template <>
-cudaError_t adj3f_dispatch<114, 12, 2, 5, 11, 1>(const AdjArgs& a, size_t smem, cudaStream_t s) {
-  return adj3_dispatch_impl_pref<114, 12, 2, 5, 11, 1, true>(a, smem, s);
 }
 
 }  // namespace wg

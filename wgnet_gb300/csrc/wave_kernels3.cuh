@@ -78,11 +78,13 @@ __device__ __forceinline__ int light_tid(int tid, int rank) {
   return (tid - ls * SEGT + NT) % NT;
 }
 
-// Fast arithmetic (FA kernels): the reference's stencils with 1/h and 1/h^2 folded into the weights
-// and the products fused (fmaf rounds once). The same discrete operators as the reference's
-// operation order, rounded differently: results agree with the unfused kernels to f32 accuracy,
-// not bit for bit. Weights: k0 = -5/2 / h^2, k1 = 4/3 / h^2, k2 = -1/12 / h^2 (second difference),
-// e1 = 2/3 / h, e2 = -1/12 / h (first difference); the adjoint's stencils carry the same numbers.
+// Fast arithmetic (the forward's FA kernels): the reference's stencils with 1/h and 1/h^2 folded
+// into the weights and the products fused (fmaf rounds once). The same discrete operator as the
+// reference's operation order, rounded differently: results agree with the unfused kernels to f32
+// accuracy, not bit for bit. Weights: k0 = -5/2 / h^2, k1 = 4/3 / h^2, k2 = -1/12 / h^2 (second
+// difference), e1 = 2/3 / h, e2 = -1/12 / h (first difference). The adjoint keeps the reference
+// order: a fused variant of it measured 1.3 % slower than the unfused one (its longer dependency
+// chains cost more than its 11 % fewer instructions save), so it was not kept.
 struct FastCoef {
   float k0, k1, k2, k00, e1, e2;
   __device__ __forceinline__ static FastCoef make(float rh) {
@@ -564,7 +566,7 @@ __global__ void __launch_bounds__(NSEG * 32 * (1 + NI), 1) fwd3_kernel(const __g
 // ------------------------------------------------------------------------------------------------
 // PREF: fetch the next step's stored gradient terms between the barrier's arrive and wait (2 S more
 // registers per thread) instead of loading each row's terms when the row is processed.
-template <int NX, int PMLP, int C, int S, int NSEG, int NI, int LAY, bool PREF, bool FA = false>
+template <int NX, int PMLP, int C, int S, int NSEG, int NI, int LAY, bool PREF>
 __global__ void __launch_bounds__(NSEG * 32 * (1 + NI), 1) adj3_kernel(const __grid_constant__ AdjArgs p) {
   using CL = Cols3<NX, PMLP>;
   constexpr int SW = CL::SW;
@@ -576,7 +578,6 @@ __global__ void __launch_bounds__(NSEG * 32 * (1 + NI), 1) adj3_kernel(const __g
   const int nz = SQ ? NX : g.nz;                                                     // compile-time if square
   const int swa = g.swa, region = g.region_adj, nrec = p.st.nrec, nt = g.nt;
   const float rh = g.rh, dt2 = g.dt2;
-  const FastCoef fc = FastCoef::make(rh);
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int seg = warp / (1 + NI), wk = warp_role<NI>(warp);
   const int rank = (C > 1) ? static_cast<int>(cluster_rank()) : 0;
@@ -605,7 +606,13 @@ __global__ void __launch_bounds__(NSEG * 32 * (1 + NI), 1) adj3_kernel(const __g
   const int zb = r0 + seg * S;
   const int nrows = CL::active(wk, lane) ? (FULL ? S : max(0, min(S, r1 - zb))) : 0;
   const bool pusher = (C > 1) && nrows > 0 && ((rank > 0 && zb < r0 + FD_PAD) || (rank < C - 1 && zb + nrows > r1 - FD_PAD));
-  const bool xedge = !pml && (x < SW || x + 1 >= NX - SW);  // interior pair inside a T/U1 strip
+  // The PML warp's stencil reaches two columns past its own on the interior side: the pair next to
+  // the interior on the left strip reads x + 2, x + 3, the one on the right strip x - 2, x - 1.
+  // There b = db = 0 and the adjoint psi, zeta are zero, so the strip terms are T = VS and U1 = 0
+  // (T = 1 VS + 0 zeta differs from VS at most in the sign of a zero): those two lanes read VS
+  // instead, so only the PML warp derives strip terms for the x strips.
+  const bool edge_r = pml && (x + 2 == FD_PAD + CL::PCOLS);
+  const bool edge_l = pml && (x == NX - FD_PAD - CL::PCOLS);
   const int vbase = (zb - zl0) * NX + x;
   const int abase = (zb - r0) * 2 * SW + CL::strip(x);
   const int zsh = (zb < nz / 2) ? 0 : (nz - swa - bot_off);
@@ -764,8 +771,7 @@ __global__ void __launch_bounds__(NSEG * 32 * (1 + NI), 1) adj3_kernel(const __g
     const float* VSb = sm + L.off_vs + b * vstride;
     auto put = [&](float* __restrict__ TXb, float* __restrict__ U1Xb, float* __restrict__ TZb,
                    float* __restrict__ U1Zb) {
-      const bool xs = pml || xedge;
-      // outside the adjoint region (xedge) b = db = 0 and the adjoint psi, zeta are zero
+      const bool xs = pml;
       const float2 o = xs ? lds2(sOPB + x) : make_float2(0.f, 0.f);
       const float2 bx = xs ? lds2(sBX + x) : make_float2(0.f, 0.f);
       const float2 db = xs ? lds2(sDBX + x) : make_float2(0.f, 0.f);
@@ -778,36 +784,22 @@ __global__ void __launch_bounds__(NSEG * 32 * (1 + NI), 1) adj3_kernel(const __g
           const float2 vs = lds2(VSb + vbase + i * NX);
           const float vs0 = vs.x, vs1 = vs.y;
           if (xs) {
-            const float2 Z = pml ? lds2(LZX + i * 2 * SW) : make_float2(0.f, 0.f);
-            const float2 P = pml ? lds2(LPX + i * 2 * SW) : make_float2(0.f, 0.f);
-            if constexpr (FA) {
-              const float T0 = fmaf(o.x, vs0, bx.x * Z.x);
-              const float T1 = fmaf(o.y, vs1, bx.y * Z.y);
-              sts2(TXb + i * 2 * SW, T0, T1);
-              sts2(U1Xb + i * 2 * SW, fmaf(db.x, T0, bx.x * P.x), fmaf(db.y, T1, bx.y * P.y));
-            } else {
-              const float T0 = (o.x * vs0) + (bx.x * Z.x);
-              const float T1 = (o.y * vs1) + (bx.y * Z.y);
-              sts2(TXb + i * 2 * SW, T0, T1);
-              sts2(U1Xb + i * 2 * SW, (db.x * T0) + (bx.x * P.x), (db.y * T1) + (bx.y * P.y));
-            }
+            const float2 Z = lds2(LZX + i * 2 * SW);
+            const float2 P = lds2(LPX + i * 2 * SW);
+            const float T0 = (o.x * vs0) + (bx.x * Z.x);
+            const float T1 = (o.y * vs1) + (bx.y * Z.y);
+            sts2(TXb + i * 2 * SW, T0, T1);
+            sts2(U1Xb + i * 2 * SW, (db.x * T0) + (bx.x * P.x), (db.y * T1) + (bx.y * P.y));
           }
           if (zstrip) {
             const float bz = sBZ[z], dbz = sDBZ[z];
             const float opbz = 1.0f + bz;
             const float2 Z = lds2(LZZ + i * NX);
             const float2 P = lds2(LPZ + i * NX);
-            if constexpr (FA) {
-              const float T0 = fmaf(opbz, vs0, bz * Z.x);
-              const float T1 = fmaf(opbz, vs1, bz * Z.y);
-              sts2(TZb + i * NX, T0, T1);
-              sts2(U1Zb + i * NX, fmaf(dbz, T0, bz * P.x), fmaf(dbz, T1, bz * P.y));
-            } else {
-              const float T0 = (opbz * vs0) + (bz * Z.x);
-              const float T1 = (opbz * vs1) + (bz * Z.y);
-              sts2(TZb + i * NX, T0, T1);
-              sts2(U1Zb + i * NX, (dbz * T0) + (bz * P.x), (dbz * T1) + (bz * P.y));
-            }
+            const float T0 = (opbz * vs0) + (bz * Z.x);
+            const float T1 = (opbz * vs1) + (bz * Z.y);
+            sts2(TZb + i * NX, T0, T1);
+            sts2(U1Zb + i * NX, (dbz * T0) + (bz * P.x), (dbz * T1) + (bz * P.y));
           }
         }
       }
@@ -848,133 +840,67 @@ __global__ void __launch_bounds__(NSEG * 32 * (1 + NI), 1) adj3_kernel(const __g
       if (i < nrows) {
         const int z = zb + i;
         const float2 Vb = lds2(VSd + i * NX);  // own v^2 dt^2 lambda
-        float n0, n1;
-        if constexpr (FA) {
-          const bool zpml = z < region || z >= nz - region;
-          // x part first (as the unfused kernel), so the neighbours' loads are issued early
-          float w0 = 0.f, w1 = 0.f, sx10 = 0.f, sx11 = 0.f, sx20 = 0.f, sx21 = 0.f;
-          if (pml) {
-            const float2 Ta = lds2(TXd + i * 2 * SW - 2), Tb = lds2(TXd + i * 2 * SW), Tc = lds2(TXd + i * 2 * SW + 2);
-            const float2 Ua = lds2(U1Xd + i * 2 * SW - 2), Ub = lds2(U1Xd + i * 2 * SW),
-                         Uc = lds2(U1Xd + i * 2 * SW + 2);
-            const float2 Oa = lds2(sOPB + x - 2), Ob = lds2(sOPB + x), Oc = lds2(sOPB + x + 2);
-            const float q0 = Oa.x * Ta.x, q1 = Oa.y * Ta.y, q2 = Ob.x * Tb.x, q3 = Ob.y * Tb.y, q4 = Oc.x * Tc.x,
-                        q5 = Oc.y * Tc.y;
-            // cell x: neighbours x-2..x+2 = (Ta.x, Ta.y, Tb.x, Tb.y, Tc.x); cell x+1: (Ta.y .. Tc.y)
-            w0 = fc.d2(q2, q3 + q1, q4 + q0) - fc.d1(Ub.y - Ua.y, Uc.x - Ua.x);
-            w1 = fc.d2(q3, q4 + q2, q5 + q1) - fc.d1(Uc.x - Ub.x, Uc.y - Ua.y);
-            const float dt0 = fc.d1(Tb.y - Ta.y, Tc.x - Ta.x);
-            const float dt1 = fc.d1(Tc.x - Tb.x, Tc.y - Ta.y);
-            const float2 P = lds2(LPX + i * 2 * SW);
-            const float2 Z = lds2(LZX + i * 2 * SW);
-            const float2 a = lds2(sAX + x);
-            sts2(LPX + i * 2 * SW, a.x * (P.x - dt0), a.y * (P.y - dt1));
-            sts2(LZX + i * 2 * SW, a.x * (Vb.x + Z.x), a.y * (Vb.y + Z.y));
-          } else {
-            const float2 Va = lds2(VSd + i * NX - 2), Vc = lds2(VSd + i * NX + 2);
-            sx10 = Vb.y + Va.y;
-            sx20 = Vc.x + Va.x;
-            sx11 = Vc.x + Vb.x;
-            sx21 = Vc.y + Va.y;
-          }
-          if (zpml) {
-            const float2 Tm2 = lds2(TZd + (i - 2) * NX), Tm1 = lds2(TZd + (i - 1) * NX), T0 = lds2(TZd + i * NX),
-                         Tp1 = lds2(TZd + (i + 1) * NX), Tp2 = lds2(TZd + (i + 2) * NX);
-            const float2 Um2 = lds2(U1Zd + (i - 2) * NX), Um1 = lds2(U1Zd + (i - 1) * NX),
-                         Up1 = lds2(U1Zd + (i + 1) * NX), Up2 = lds2(U1Zd + (i + 2) * NX);
-            const float om2 = 1.0f + sBZ[z - 2], om1 = 1.0f + sBZ[z - 1], o0 = 1.0f + sBZ[z], op1 = 1.0f + sBZ[z + 1],
-                        op2 = 1.0f + sBZ[z + 2];
-            const float wz0 = fc.d2(o0 * T0.x, fmaf(op1, Tp1.x, om1 * Tm1.x), fmaf(op2, Tp2.x, om2 * Tm2.x)) -
-                              fc.d1(Up1.x - Um1.x, Up2.x - Um2.x);
-            const float wz1 = fc.d2(o0 * T0.y, fmaf(op1, Tp1.y, om1 * Tm1.y), fmaf(op2, Tp2.y, om2 * Tm2.y)) -
-                              fc.d1(Up1.y - Um1.y, Up2.y - Um2.y);
-            const float dt0 = fc.d1(Tp1.x - Tm1.x, Tp2.x - Tm2.x);
-            const float dt1 = fc.d1(Tp1.y - Tm1.y, Tp2.y - Tm2.y);
-            const float az = sAZ[z];
-            const float2 P = lds2(LPZ + i * NX);
-            const float2 Z = lds2(LZZ + i * NX);
-            sts2(LPZ + i * NX, az * (P.x - dt0), az * (P.y - dt1));
-            sts2(LZZ + i * NX, az * (Vb.x + Z.x), az * (Vb.y + Z.y));
-            if (pml) {
-              w0 = w0 + wz0;
-              w1 = w1 + wz1;
-            } else {
-              w0 = fc.d2acc(wz0, Vb.x, sx10, sx20);
-              w1 = fc.d2acc(wz1, Vb.y, sx11, sx21);
-            }
-          } else {
-            const float2 Vm2 = lds2(VSd + (i - 2) * NX), Vm1 = lds2(VSd + (i - 1) * NX), Vp1 = lds2(VSd + (i + 1) * NX),
-                         Vp2 = lds2(VSd + (i + 2) * NX);
-            if (pml) {
-              w0 = fc.d2acc(w0, Vb.x, Vp1.x + Vm1.x, Vp2.x + Vm2.x);
-              w1 = fc.d2acc(w1, Vb.y, Vp1.y + Vm1.y, Vp2.y + Vm2.y);
-            } else {
-              w0 = fc.lap(Vb.x, sx10 + (Vp1.x + Vm1.x), sx20 + (Vp2.x + Vm2.x));
-              w1 = fc.lap(Vb.y, sx11 + (Vp1.y + Vm1.y), sx21 + (Vp2.y + Vm2.y));
-            }
-          }
-          n0 = fmaf(2.0f, lc[i][0], w0 - lp[i][0]);
-          n1 = fmaf(2.0f, lc[i][1], w1 - lp[i][1]);
+        float w0, w1;
+        if (pml) {
+          const float2 Ta = lds2(edge_l ? VSd + i * NX - 2 : TXd + i * 2 * SW - 2), Tb = lds2(TXd + i * 2 * SW),
+                       Tc = lds2(edge_r ? VSd + i * NX + 2 : TXd + i * 2 * SW + 2);
+          float2 Ua = lds2(U1Xd + i * 2 * SW - 2), Uc = lds2(U1Xd + i * 2 * SW + 2);
+          const float2 Ub = lds2(U1Xd + i * 2 * SW);
+          if (edge_l) Ua = make_float2(0.f, 0.f);
+          if (edge_r) Uc = make_float2(0.f, 0.f);
+          const float2 Oa = lds2(sOPB + x - 2), Ob = lds2(sOPB + x), Oc = lds2(sOPB + x + 2);
+          const float q0 = Oa.x * Ta.x, q1 = Oa.y * Ta.y, q2 = Ob.x * Tb.x, q3 = Ob.y * Tb.y, q4 = Oc.x * Tc.x,
+                      q5 = Oc.y * Tc.y;
+          // cell x: neighbours x-2..x+2 = (Ta.x, Ta.y, Tb.x, Tb.y, Tc.x)
+          const float du0 = ((F_D1A * (Ub.y - Ua.y)) + (A_D1B * (Uc.x - Ua.x))) * rh;
+          const float dd0 = ((((F_D2A * q2) + (F_D2B * (q3 + q1))) + (A_D2C * (q4 + q0))) * rh) * rh;
+          const float dt0 = ((F_D1A * (Tb.y - Ta.y)) + (A_D1B * (Tc.x - Ta.x))) * rh;
+          // cell x+1: neighbours x-1..x+3 = (Ta.y, Tb.x, Tb.y, Tc.x, Tc.y)
+          const float du1 = ((F_D1A * (Uc.x - Ub.x)) + (A_D1B * (Uc.y - Ua.y))) * rh;
+          const float dd1 = ((((F_D2A * q3) + (F_D2B * (q4 + q2))) + (A_D2C * (q5 + q1))) * rh) * rh;
+          const float dt1 = ((F_D1A * (Tc.x - Tb.x)) + (A_D1B * (Tc.y - Ta.y))) * rh;
+          w0 = (-du0) + dd0;
+          w1 = (-du1) + dd1;
+          const float2 P = lds2(LPX + i * 2 * SW);
+          const float2 Z = lds2(LZX + i * 2 * SW);
+          const float2 a = lds2(sAX + x);
+          sts2(LPX + i * 2 * SW, ((-a.x) * dt0) + (a.x * P.x), ((-a.y) * dt1) + (a.y * P.y));
+          sts2(LZX + i * 2 * SW, (a.x * Vb.x) + (a.x * Z.x), (a.y * Vb.y) + (a.y * Z.y));
         } else {
-          float w0, w1;
-          if (pml) {
-            const float2 Ta = lds2(TXd + i * 2 * SW - 2), Tb = lds2(TXd + i * 2 * SW), Tc = lds2(TXd + i * 2 * SW + 2);
-            const float2 Ua = lds2(U1Xd + i * 2 * SW - 2), Ub = lds2(U1Xd + i * 2 * SW),
-                         Uc = lds2(U1Xd + i * 2 * SW + 2);
-            const float2 Oa = lds2(sOPB + x - 2), Ob = lds2(sOPB + x), Oc = lds2(sOPB + x + 2);
-            const float q0 = Oa.x * Ta.x, q1 = Oa.y * Ta.y, q2 = Ob.x * Tb.x, q3 = Ob.y * Tb.y, q4 = Oc.x * Tc.x,
-                        q5 = Oc.y * Tc.y;
-            // cell x: neighbours x-2..x+2 = (Ta.x, Ta.y, Tb.x, Tb.y, Tc.x)
-            const float du0 = ((F_D1A * (Ub.y - Ua.y)) + (A_D1B * (Uc.x - Ua.x))) * rh;
-            const float dd0 = ((((F_D2A * q2) + (F_D2B * (q3 + q1))) + (A_D2C * (q4 + q0))) * rh) * rh;
-            const float dt0 = ((F_D1A * (Tb.y - Ta.y)) + (A_D1B * (Tc.x - Ta.x))) * rh;
-            // cell x+1: neighbours x-1..x+3 = (Ta.y, Tb.x, Tb.y, Tc.x, Tc.y)
-            const float du1 = ((F_D1A * (Uc.x - Ub.x)) + (A_D1B * (Uc.y - Ua.y))) * rh;
-            const float dd1 = ((((F_D2A * q3) + (F_D2B * (q4 + q2))) + (A_D2C * (q5 + q1))) * rh) * rh;
-            const float dt1 = ((F_D1A * (Tc.x - Tb.x)) + (A_D1B * (Tc.y - Ta.y))) * rh;
-            w0 = (-du0) + dd0;
-            w1 = (-du1) + dd1;
-            const float2 P = lds2(LPX + i * 2 * SW);
-            const float2 Z = lds2(LZX + i * 2 * SW);
-            const float2 a = lds2(sAX + x);
-            sts2(LPX + i * 2 * SW, ((-a.x) * dt0) + (a.x * P.x), ((-a.y) * dt1) + (a.y * P.y));
-            sts2(LZX + i * 2 * SW, (a.x * Vb.x) + (a.x * Z.x), (a.y * Vb.y) + (a.y * Z.y));
-          } else {
-            const float2 Va = lds2(VSd + i * NX - 2), Vc = lds2(VSd + i * NX + 2);
-            w0 = ((((F_D2A * Vb.x) + (F_D2B * (Vb.y + Va.y))) + (A_D2C * (Vc.x + Va.x))) * rh) * rh;
-            w1 = ((((F_D2A * Vb.y) + (F_D2B * (Vc.x + Vb.x))) + (A_D2C * (Vc.y + Va.y))) * rh) * rh;
-          }
-          if (z < region || z >= nz - region) {
-            const float2 Tm2 = lds2(TZd + (i - 2) * NX), Tm1 = lds2(TZd + (i - 1) * NX), T0 = lds2(TZd + i * NX),
-                         Tp1 = lds2(TZd + (i + 1) * NX), Tp2 = lds2(TZd + (i + 2) * NX);
-            const float2 Um2 = lds2(U1Zd + (i - 2) * NX), Um1 = lds2(U1Zd + (i - 1) * NX),
-                         Up1 = lds2(U1Zd + (i + 1) * NX), Up2 = lds2(U1Zd + (i + 2) * NX);
-            const float om2 = 1.0f + sBZ[z - 2], om1 = 1.0f + sBZ[z - 1], o0 = 1.0f + sBZ[z], op1 = 1.0f + sBZ[z + 1],
-                        op2 = 1.0f + sBZ[z + 2];
-            const float du0 = ((F_D1A * (Up1.x - Um1.x)) + (A_D1B * (Up2.x - Um2.x))) * rh;
-            const float du1 = ((F_D1A * (Up1.y - Um1.y)) + (A_D1B * (Up2.y - Um2.y))) * rh;
-            const float dd0 = ((((F_D2A * (o0 * T0.x)) + (F_D2B * ((op1 * Tp1.x) + (om1 * Tm1.x)))) +
-                                (A_D2C * ((op2 * Tp2.x) + (om2 * Tm2.x)))) * rh) * rh;
-            const float dd1 = ((((F_D2A * (o0 * T0.y)) + (F_D2B * ((op1 * Tp1.y) + (om1 * Tm1.y)))) +
-                                (A_D2C * ((op2 * Tp2.y) + (om2 * Tm2.y)))) * rh) * rh;
-            const float dt0 = ((F_D1A * (Tp1.x - Tm1.x)) + (A_D1B * (Tp2.x - Tm2.x))) * rh;
-            const float dt1 = ((F_D1A * (Tp1.y - Tm1.y)) + (A_D1B * (Tp2.y - Tm2.y))) * rh;
-            w0 = w0 + ((-du0) + dd0);
-            w1 = w1 + ((-du1) + dd1);
-            const float az = sAZ[z];
-            const float2 P = lds2(LPZ + i * NX);
-            const float2 Z = lds2(LZZ + i * NX);
-            sts2(LPZ + i * NX, ((-az) * dt0) + (az * P.x), ((-az) * dt1) + (az * P.y));
-            sts2(LZZ + i * NX, (az * Vb.x) + (az * Z.x), (az * Vb.y) + (az * Z.y));
-          } else {
-            const float2 Vm2 = lds2(VSd + (i - 2) * NX), Vm1 = lds2(VSd + (i - 1) * NX), Vp1 = lds2(VSd + (i + 1) * NX),
-                         Vp2 = lds2(VSd + (i + 2) * NX);
-            w0 = w0 + ((((F_D2A * Vb.x) + (F_D2B * (Vp1.x + Vm1.x))) + (A_D2C * (Vp2.x + Vm2.x))) * rh) * rh;
-            w1 = w1 + ((((F_D2A * Vb.y) + (F_D2B * (Vp1.y + Vm1.y))) + (A_D2C * (Vp2.y + Vm2.y))) * rh) * rh;
-          }
-          n0 = (w0 + (2.0f * lc[i][0])) - lp[i][0];
-          n1 = (w1 + (2.0f * lc[i][1])) - lp[i][1];
+          const float2 Va = lds2(VSd + i * NX - 2), Vc = lds2(VSd + i * NX + 2);
+          w0 = ((((F_D2A * Vb.x) + (F_D2B * (Vb.y + Va.y))) + (A_D2C * (Vc.x + Va.x))) * rh) * rh;
+          w1 = ((((F_D2A * Vb.y) + (F_D2B * (Vc.x + Vb.x))) + (A_D2C * (Vc.y + Va.y))) * rh) * rh;
         }
+        if (z < region || z >= nz - region) {
+          const float2 Tm2 = lds2(TZd + (i - 2) * NX), Tm1 = lds2(TZd + (i - 1) * NX), T0 = lds2(TZd + i * NX),
+                       Tp1 = lds2(TZd + (i + 1) * NX), Tp2 = lds2(TZd + (i + 2) * NX);
+          const float2 Um2 = lds2(U1Zd + (i - 2) * NX), Um1 = lds2(U1Zd + (i - 1) * NX),
+                       Up1 = lds2(U1Zd + (i + 1) * NX), Up2 = lds2(U1Zd + (i + 2) * NX);
+          const float om2 = 1.0f + sBZ[z - 2], om1 = 1.0f + sBZ[z - 1], o0 = 1.0f + sBZ[z], op1 = 1.0f + sBZ[z + 1],
+                      op2 = 1.0f + sBZ[z + 2];
+          const float du0 = ((F_D1A * (Up1.x - Um1.x)) + (A_D1B * (Up2.x - Um2.x))) * rh;
+          const float du1 = ((F_D1A * (Up1.y - Um1.y)) + (A_D1B * (Up2.y - Um2.y))) * rh;
+          const float dd0 = ((((F_D2A * (o0 * T0.x)) + (F_D2B * ((op1 * Tp1.x) + (om1 * Tm1.x)))) +
+                              (A_D2C * ((op2 * Tp2.x) + (om2 * Tm2.x)))) * rh) * rh;
+          const float dd1 = ((((F_D2A * (o0 * T0.y)) + (F_D2B * ((op1 * Tp1.y) + (om1 * Tm1.y)))) +
+                              (A_D2C * ((op2 * Tp2.y) + (om2 * Tm2.y)))) * rh) * rh;
+          const float dt0 = ((F_D1A * (Tp1.x - Tm1.x)) + (A_D1B * (Tp2.x - Tm2.x))) * rh;
+          const float dt1 = ((F_D1A * (Tp1.y - Tm1.y)) + (A_D1B * (Tp2.y - Tm2.y))) * rh;
+          w0 = w0 + ((-du0) + dd0);
+          w1 = w1 + ((-du1) + dd1);
+          const float az = sAZ[z];
+          const float2 P = lds2(LPZ + i * NX);
+          const float2 Z = lds2(LZZ + i * NX);
+          sts2(LPZ + i * NX, ((-az) * dt0) + (az * P.x), ((-az) * dt1) + (az * P.y));
+          sts2(LZZ + i * NX, (az * Vb.x) + (az * Z.x), (az * Vb.y) + (az * Z.y));
+        } else {
+          const float2 Vm2 = lds2(VSd + (i - 2) * NX), Vm1 = lds2(VSd + (i - 1) * NX), Vp1 = lds2(VSd + (i + 1) * NX),
+                       Vp2 = lds2(VSd + (i + 2) * NX);
+          w0 = w0 + ((((F_D2A * Vb.x) + (F_D2B * (Vp1.x + Vm1.x))) + (A_D2C * (Vp2.x + Vm2.x))) * rh) * rh;
+          w1 = w1 + ((((F_D2A * Vb.y) + (F_D2B * (Vp1.y + Vm1.y))) + (A_D2C * (Vp2.y + Vm2.y))) * rh) * rh;
+        }
+        float n0 = (w0 + (2.0f * lc[i][0])) - lp[i][0];
+        float n1 = (w1 + (2.0f * lc[i][1])) - lp[i][1];
         const float2 sv = PREF ? stv[PREF ? i : 0] : __ldcs(reinterpret_cast<const float2*>(st_t + i * NX));
         // the shader starts the per-step gradient at +0; starting from the product itself differs
         // only in the sign of an exact zero
@@ -1009,10 +935,7 @@ __global__ void __launch_bounds__(NSEG * 32 * (1 + NI), 1) adj3_kernel(const __g
         }
         {
           const float2 ga = lds2(GAo + i * NX);
-          if (FA && !(wsrc & (3u << (2 * i))))  // fused when the row holds no source
-            sts2(GAo + i * NX, fmaf(lc[i][0], sv.x, ga.x), fmaf(lc[i][1], sv.y, ga.y));
-          else
-            sts2(GAo + i * NX, ga.x + g0, ga.y + g1);
+          sts2(GAo + i * NX, ga.x + g0, ga.y + g1);
         }
         lp[i][0] = n0;
         lp[i][1] = n1;
@@ -1117,20 +1040,20 @@ cudaError_t fwd3_dispatch_impl(bool traces, bool store, const FwdArgs& a, size_t
   return fwd3_launch<NX, PMLP, C, S, NSEG, NI, LAY_RUNTIME, FA>(traces, store, a, smem, s);
 }
 
-template <int NX, int PMLP, int C, int S, int NSEG, int NI, bool PREF, bool FA>
+template <int NX, int PMLP, int C, int S, int NSEG, int NI, bool PREF>
 cudaError_t adj3_dispatch_impl(const AdjArgs& a, size_t smem, cudaStream_t s) {
   constexpr int NT = NSEG * 32 * (1 + NI);
   constexpr int LAY_FAST = NI == 1 ? LAY_SQUARE : LAY_EVEN;
   if (g3_layout<NX, C, S, NSEG, NI>(a.g.nz) == LAY_FAST)
-    return launch_cluster(adj3_kernel<NX, PMLP, C, S, NSEG, NI, LAY_FAST, PREF, FA>, C, NT, a.units, smem, s, a);
-  return launch_cluster(adj3_kernel<NX, PMLP, C, S, NSEG, NI, LAY_RUNTIME, PREF, FA>, C, NT, a.units, smem, s, a);
+    return launch_cluster(adj3_kernel<NX, PMLP, C, S, NSEG, NI, LAY_FAST, PREF>, C, NT, a.units, smem, s, a);
+  return launch_cluster(adj3_kernel<NX, PMLP, C, S, NSEG, NI, LAY_RUNTIME, PREF>, C, NT, a.units, smem, s, a);
 }
 
 // Adjoint launch: the prefetching variant when `pref` is set in the shape.
-template <int NX, int PMLP, int C, int S, int NSEG, int NI, bool FA = false>
+template <int NX, int PMLP, int C, int S, int NSEG, int NI>
 cudaError_t adj3_dispatch_impl_pref(const AdjArgs& a, size_t smem, cudaStream_t s) {
-  if (a.prefetch) return adj3_dispatch_impl<NX, PMLP, C, S, NSEG, NI, true, FA>(a, smem, s);
-  return adj3_dispatch_impl<NX, PMLP, C, S, NSEG, NI, false, FA>(a, smem, s);
+  if (a.prefetch) return adj3_dispatch_impl<NX, PMLP, C, S, NSEG, NI, true>(a, smem, s);
+  return adj3_dispatch_impl<NX, PMLP, C, S, NSEG, NI, false>(a, smem, s);
 }
 
 }  // namespace wg

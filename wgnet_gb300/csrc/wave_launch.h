@@ -31,11 +31,9 @@ template <int NX, int PMLP, int C, int S, int NSEG, int NI>
 cudaError_t fwd3_dispatch(bool traces, bool store, const FwdArgs& a, size_t smem, cudaStream_t s);
 template <int NX, int PMLP, int C, int S, int NSEG, int NI>
 cudaError_t adj3_dispatch(const AdjArgs& a, size_t smem, cudaStream_t s);
-// fast-arithmetic variants, compiled for the shapes of WG_G3_FAST_SHAPES (wave_table.cu)
+// fast-arithmetic forward, compiled for the shapes of WG_G3_FAST_SHAPES (wave_table.cu)
 template <int NX, int PMLP, int C, int S, int NSEG, int NI>
 cudaError_t fwd3f_dispatch(bool traces, bool store, const FwdArgs& a, size_t smem, cudaStream_t s);
-template <int NX, int PMLP, int C, int S, int NSEG, int NI>
-cudaError_t adj3f_dispatch(const AdjArgs& a, size_t smem, cudaStream_t s);
 
 // Forward over units = models * shots. traces: record receivers; store: write 2 v dt^2 w.
 cudaError_t launch_fwd(const Shape& s, bool traces, bool store, const FwdArgs& a, cudaStream_t stream);

@@ -31,7 +31,7 @@ namespace wg {
   X(184, 12, 6, 6, 5, 3)        \
   X(184, 12, 6, 10, 3, 3)
 
-// generation-3 shapes that also have fast-arithmetic kernels (one instantiation file each): the
+// generation-3 shapes that also have a fast-arithmetic forward (one instantiation file each): the
 // default shape of each of the 70x70, 100x100 and 140x140 grids at pml 20
 #define WG_G3_FAST_SHAPES(X)    \
   X(114, 12, 2, 5, 11, 1)       \
@@ -155,13 +155,6 @@ cudaError_t launch_fwd(const Shape& s, bool traces, bool store, const FwdArgs& a
 cudaError_t launch_adj(const Shape& s, const AdjArgs& a, cudaStream_t stream) {
   const size_t smem = adj_smem_bytes(s, a.g.nx, a.g.nz, a.g.swa, a.st.nrec);
   if (s.kind == 3) {
-    if (a.fast) {
-#define WG_ADJ3F(NXs, PMLPs, Cc, Ss, NSEGs, NIs)                                                                 \
-  if (s.nxc == NXs && s.pmlp == PMLPs && s.cluster == Cc && s.seg_rows == Ss && s.nseg == NSEGs && s.ni == NIs) \
-    return adj3f_dispatch<NXs, PMLPs, Cc, Ss, NSEGs, NIs>(a, smem, stream);
-      WG_G3_FAST_SHAPES(WG_ADJ3F)
-#undef WG_ADJ3F
-    }
 #define WG_ADJ3(NXs, PMLPs, Cc, Ss, NSEGs, NIs)                                                                  \
   if (s.nxc == NXs && s.pmlp == PMLPs && s.cluster == Cc && s.seg_rows == Ss && s.nseg == NSEGs && s.ni == NIs) \
     return adj3_dispatch<NXs, PMLPs, Cc, Ss, NSEGs, NIs>(a, smem, stream);
