@@ -45,7 +45,25 @@ UPDATED_CELLS = (NX + 2 * (PML + 2) - 4) ** 2  # 110 x 110 cells updated per ste
 FLOPS_PER_CELL_UPDATE = 48.0  # average over interior / one-PML-axis / two-PML-axes cells at pml 20
 # DRAM bytes per (unit, step) measured with ncu on the small case (32 models, nt 200: the full
 # 256-model launch is too large for a multi-pass capture), scaled by unit-steps to a full launch
-MEASURED_TRAFFIC_PER_UNIT_STEP = {"adjoint": (813.22e6 + 9.68e6) / 16000, "recompute": (69.83e6 + 736.70e6) / 16000}
+MEASURED_TRAFFIC_PER_UNIT_STEP = {"adjoint": (813.03e6 + 9.72e6) / 16000, "recompute": (69.93e6 + 736.38e6) / 16000}
+# Counters of the same small-case captures (ncu --set full), per kernel: thread-instructions per
+# updated cell and step, issue slots busy, L1/shared throughput, shared-memory bank-conflict share.
+NCU_SMALL_CASE = {
+    "adjoint": {"thread_instructions_per_cell_update": None, "issue_active_pct": 60.8, "l1_shared_pct": 66.3,
+                "bank_conflict_pct_of_shared_wavefronts": 0.6},
+    "recompute": {"thread_instructions_per_cell_update": None, "issue_active_pct": 54.8, "l1_shared_pct": 56.6,
+                  "bank_conflict_pct_of_shared_wavefronts": 3.2},
+}
+def flops_per_cell_update(n_vis: int, pml: int = PML) -> float:
+    """Algorithmic flops per updated cell and step of the forward (lib.rs:158-205; add, sub, mul 1,
+    FMA 2): 24 in the interior, 54 with one C-PML axis, 84 with two, averaged over the updated
+    square grid whose C-PML strips are pml + 2 cells wide on each side (48.0 at 70 x 70, pml 20)."""
+    n = n_vis + 2 * (pml + 2) - 4
+    p = 2 * (pml + 2)
+    return (84.0 * p * p + 54.0 * 2 * p * (n - p) + 24.0 * (n - p) ** 2) / (n * n)
+
+
+FP32_LANES_PER_SM = 128  # FP32 lanes of a Blackwell SM (two dies x 76 SMs on GB300)
 
 
 def clocks_sampler(stop: threading.Event, out: list):
@@ -216,7 +234,7 @@ def run_datagen(args):
         fms, fl = eng.profile_read()["forward"]
         eng.profile(False)
         upd = (eng.nx - 4) * (eng.nz - 4)
-        f = counts[n] * SHOTS * args.nt * upd * FLOPS_PER_CELL_UPDATE
+        f = counts[n] * SHOTS * args.nt * upd * flops_per_cell_update(n)
         flops += f
         per_grid[str(n)] = {"models": counts[n], "forward_ms": fms, "launches": fl, "launch_shape": gen.shapes[n],
                             "gcell_updates_per_s": counts[n] * SHOTS * args.nt * upd / (fms / 1000.0) / 1e9}
@@ -224,8 +242,12 @@ def run_datagen(args):
     dn = int(dom)
     dom_ms = per_grid[dom]["forward_ms"]
     dom_bytes = counts[dn] * SHOTS * (args.nt * dn * 4 + (dn + 44) ** 2 * 4)
+    dom_flops = counts[dn] * SHOTS * args.nt * (dn + 40) ** 2 * flops_per_cell_update(dn)
     hbm_peak, peak_kind = measured_peaks()
     props = torch.cuda.get_device_properties(0)
+    clocks = summarize_clocks(clk)
+    sm_mhz = clocks["sm_mhz"] or 2070.0
+    fp32_peak = props.multi_processor_count * FP32_LANES_PER_SM * 2 * sm_mhz * 1e6 / 1e12
     line = {
         "metric": DATAGEN_METRIC, "value": value, "unit": DATAGEN_UNIT, "n_gpus": 1, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
@@ -237,13 +259,17 @@ def run_datagen(args):
         "e2e": {"value": e2e, "unit": DATAGEN_UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": gen.kernels_per_launch * args.steps, "outputs_finite": ok,
         "per_grid": per_grid,
-        "roofline": {"kernel": f"forward {dom}x{dom}", "bound": "hbm",
-                     "achieved": dom_bytes / (dom_ms / 1000.0) / 1e9, "peak": hbm_peak, "unit": "GB/s",
-                     "frac": dom_bytes / (dom_ms / 1000.0) / 1e9 / hbm_peak, "peak_source": peak_kind,
-                     "traffic": None, "bytes_per_launch": dom_bytes, "avg_launch_ms": dom_ms},
-        "roofline_fp32": {"achieved_tflops": flops / (ms / args.steps / 1000.0) / 1e12,
-                          "sms": props.multi_processor_count},
-        "clocks": summarize_clocks(clk),
+        # resident forward: the wavefield stays in shared memory, so the FP32 pipe bounds it
+        "roofline": {"kernel": f"forward {dom}x{dom}", "bound": "fp32",
+                     "achieved": dom_flops / (dom_ms / 1000.0) / 1e12, "peak": fp32_peak, "unit": "TFLOP/s",
+                     "frac": dom_flops / (dom_ms / 1000.0) / 1e12 / fp32_peak,
+                     "peak_source": f"computed: {props.multi_processor_count} SMs x {FP32_LANES_PER_SM} FP32 lanes x "
+                                    f"2 flop x {sm_mhz:.0f} MHz (median SM clock of this run)",
+                     "traffic": None, "flops_per_launch": dom_flops, "avg_launch_ms": dom_ms,
+                     "hbm": {"achieved": dom_bytes / (dom_ms / 1000.0) / 1e9, "peak": hbm_peak, "unit": "GB/s",
+                             "peak_source": peak_kind, "bytes_per_launch": dom_bytes}},
+        "fp32_whole_graph_tflops": flops / (ms / args.steps / 1000.0) / 1e12,
+        "clocks": clocks,
     }
     if not args.no_cpu_baseline:
         from oracle import native as o
@@ -535,6 +561,61 @@ def run_reference_datagen(args):
     return 0
 
 
+def fast_arith_rate(args, eng, lib, d_start, d_obs, h_vel, h_obs, h_loss, h_grad, models, dist, dev, world, tune_it):
+    """The same gradient batch with the fast-arithmetic forward (engine option arith = 1: fused,
+    reassociated stencils; the adjoint keeps the reference order), timed the same way. Its results
+    are not bit-identical to the reference: gathers agree to <= 1e-5 and gradients to <= 1e-4
+    relative L2 on config 1; on a model with a small misfit the gradient agrees with the FP64
+    result as well as the FP32 reference does (tests/test_gpu_fast_arith.py)."""
+    import torch
+
+    from wgnet_gb300 import _lib, replicas
+
+    eng.set_option("arith", 1)
+    if tune_it:
+        from wgnet_gb300.autotune import tune
+
+        tune(eng)
+    for _ in range(args.warmup):
+        eng.evaluate_adjoint_torch(d_start, d_obs, check_status=False)
+    torch.cuda.synchronize()
+    replicas.barrier(dist)
+    lib.wg_profile(eng._h, 1)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record()
+    for _ in range(args.steps):
+        eng.evaluate_adjoint_torch(d_start, d_obs, check_status=False)
+    ev1.record()
+    torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1)
+    eng.status("timed gradients (fast arithmetic)")
+    kms = (ctypes.c_double * 4)()
+    kn = (ctypes.c_longlong * 4)()
+    lib.wg_profile_read(eng._h, kms, kn, 4)
+    lib.wg_profile(eng._h, 0)
+    ms = replicas.max_over_ranks(ms, dist, dev)
+    value = replicas.aggregate_rate(models, args.steps, world, ms)
+
+    def host_step():
+        _lib.check(lib.wg_evaluate_adjoint(eng._h, h_vel.data_ptr(), h_obs.data_ptr(), models, h_loss.data_ptr(),
+                                           h_grad.data_ptr()))
+
+    host_step()
+    replicas.barrier(dist)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        host_step()
+    e2e_s = replicas.max_over_ranks(time.perf_counter() - t0, dist, dev)
+    eng.set_option("arith", 0)
+    names = ["forward", "recompute", "adjoint"]
+    return {"value": value, "unit": UNIT, "ms_per_step": ms / args.steps,
+            "e2e": {"value": replicas.aggregate_rate(models, args.steps, world, e2e_s * 1000.0), "unit": UNIT},
+            "kernels_ms": {names[k]: {"total_ms": kms[k], "launches": int(kn[k])} for k in range(3)},
+            "launch_shape": {"forward": eng.launch_shape("forward"), "adjoint": eng.launch_shape("adjoint")},
+            "accuracy": "not bit-identical: gathers <= 1e-5, gradients <= 1e-4 rel L2 vs the FP32 reference on "
+                        "config 1; small-misfit models as close to FP64 as the FP32 reference"}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -546,6 +627,8 @@ def main():
     ap.add_argument("--nt", type=int, default=NT, help="time steps (profiling runs use a short record)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-autotune", action="store_true", help="keep the engine's default launch shapes")
+    ap.add_argument("--no-fast", action="store_true",
+                    help="skip the secondary measurement with the fast-arithmetic forward (arith 1)")
     ap.add_argument("--arith", default="exact", choices=["exact", "fast"],
                     help="exact: the reference's f32 operation order (bit-identical results); fast: fused, "
                          "reassociated stencils (within the stated f32 tolerances)")
@@ -666,7 +749,6 @@ def main():
     units = M * SHOTS
     seg = args.checkpoint if 0 < args.checkpoint < nt else nt
     steps_per_launch = {0: nt, 1: seg, 2: seg}[dom]
-    cells_padded = (NX + 2 * (PML + 2)) ** 2
     # algorithmic HBM bytes per launch of the dominant kernel
     if dom == 2:  # adjoint: read stored terms of every updated cell and step, residuals; state in/out
         per = units * steps_per_launch * (UPDATED_CELLS * 4 + 70 * 4)
@@ -680,6 +762,11 @@ def main():
     flops_launch = units * steps_per_launch * UPDATED_CELLS * FLOPS_PER_CELL_UPDATE
     fp32_tflops = flops_launch / (avg_ms / 1000.0) / 1e12
     cells_per_s = M * SHOTS * nt * UPDATED_CELLS * 2 / (ms_step / 1000.0)
+    clocks = summarize_clocks(clk)
+    props = torch.cuda.get_device_properties(dev)
+    sm_mhz = clocks["sm_mhz"] or 2070.0
+    fp32_peak = props.multi_processor_count * FP32_LANES_PER_SM * 2 * sm_mhz * 1e6 / 1e12
+    traffic = MEASURED_TRAFFIC_PER_UNIT_STEP.get(names[dom], 0.0) * units * steps_per_launch or None
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
@@ -696,14 +783,24 @@ def main():
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": launches,
         "kernels_ms": {names[k]: {"total_ms": kms[k], "launches": int(kn[k])} for k in range(3)},
-        "roofline": {"kernel": names[dom], "bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-                     "frac": achieved / hbm_peak, "peak_source": peak_kind,
-                     "traffic": (MEASURED_TRAFFIC_PER_UNIT_STEP.get(names[dom], 0.0) * units * steps_per_launch) or None,
-                     "bytes_per_launch": per, "avg_launch_ms": avg_ms},
-        "roofline_fp32": {"kernel": names[dom], "achieved_tflops": fp32_tflops,
-                          "flops_per_launch": flops_launch, "flops_per_cell_update": FLOPS_PER_CELL_UPDATE},
+        # The resident 70x70 kernels keep the wavefield in shared memory: FP32-pipe bound (shared
+        # memory the second bound); HBM carries only the stored gradient terms and the gathers.
+        "roofline": {"kernel": names[dom], "bound": "fp32", "achieved": fp32_tflops, "peak": fp32_peak,
+                     "unit": "TFLOP/s", "frac": fp32_tflops / fp32_peak,
+                     "peak_source": f"computed: {props.multi_processor_count} SMs x {FP32_LANES_PER_SM} FP32 lanes x "
+                                    f"2 flop x {sm_mhz:.0f} MHz (median SM clock of this run's clocks record)",
+                     "flops_per_launch": flops_launch, "flops_per_cell_update": FLOPS_PER_CELL_UPDATE,
+                     "avg_launch_ms": avg_ms, "traffic": traffic,
+                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of a 32-model nt-200 capture, "
+                                       "scaled by unit-steps",
+                     "hbm": {"achieved": achieved, "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak,
+                             "peak_source": peak_kind, "bytes_per_launch": per},
+                     "ncu_small_case": NCU_SMALL_CASE.get(names[dom])},
     }
-    line["clocks"] = summarize_clocks(clk)
+    line["clocks"] = clocks
+    if args.arith == "exact" and not args.no_fast:
+        line["fast_arith"] = fast_arith_rate(args, eng, lib, d_start, d_obs, h_vel, h_obs, h_loss, h_grad, M, dist,
+                                             dev, world, tuned is not None)
     if rank == 0 and not args.no_cpu_baseline:
         from oracle import native as o
 

@@ -256,3 +256,28 @@ def test_parametrisation_matches_reference_golden():
     cz = 2 * (s // 35)[:, None] + (k // 25 - 12)[None] + 0.5
     np.testing.assert_array_equal(centres.numpy(), np.stack([cx, cz], -1).astype(np.float32))
     assert render.slot_windows() is render.slot_windows()  # cached per device
+
+
+def test_pyo3_standin_and_reference_python_fixtures():
+    """The oracle-backed stand-in for the reference's PyO3 module keeps lib.rs's defaults, shapes and
+    errors, and the fixtures made by running the reference's Python over it meet verify.py's own
+    criteria (tests/golden/make_refpy.py)."""
+    from oracle import pyo3_standin as w
+
+    eng = w.PyWaveEngine(shots=2, nt=60)
+    assert (eng.shots, eng.nt, eng.nrec) == (2, 60, 70)
+    np.testing.assert_array_equal(eng.sources(), np.float32([[0.0, 10.0], [690.0, 10.0]]))
+    np.testing.assert_array_equal(eng.wavelet(), o.ricker(60, 0.0005, 15.0))
+    v = np.full(4900, 2500.0, np.float32)
+    assert eng.simulate(v).shape == (2, 60, 70)
+    with pytest.raises(ValueError):
+        eng.set_sources(np.zeros((3, 2), np.float32))
+    with pytest.raises(ValueError):
+        eng.simulate(np.zeros(10, np.float32))
+    with pytest.raises(TypeError):
+        eng.simulate(np.zeros(4900, np.float64))
+    g = np.load(GOLD / "refpy.npz")
+    assert int(g["ref_solves"]) == 30 and float(g["ref_final_loss"]) < 0.7 * float(g["ref_initial_loss"])
+    assert g["adj_grads"].shape == (1, 70, 70) and np.isfinite(g["adj_grads"]).all()
+    low, filt = g["band_low"], g["band_filtered"]
+    assert float(np.abs(low - filt).max() / np.abs(filt).max()) < 2e-3
