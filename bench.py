@@ -318,14 +318,14 @@ def large_bytes_per_cell_update(nx: int, nz: int, pml: int, shots: int) -> tuple
     return fwd, adj
 
 
-def run_large(args):
+def measure_large(nt: int, shots: int, steps: int, warmup: int) -> dict:
+    """The large survey's gradients on the streamed path: `steps` gradients timed with device-resident
+    inputs (CUDA events, clocks sampled), then `steps` through the host C ABI entry point."""
     import torch
 
     from wgnet_gb300 import _lib
     from wgnet_gb300.engine import WaveEngine
 
-    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
-    nt, shots = args.nt, args.shots
     true, start = large_workload(nt, shots)
     eng = WaveEngine(shots=shots, nt=nt, dt=0.0005, peak_hz=15.0, pml=PML, vmin=1000.0, vmax=5000.0, nx_vis=800,
                      nz_vis=300, h=5.0)
@@ -334,7 +334,7 @@ def run_large(args):
     d_true = torch.from_numpy(true).to(dev)
     d_obs = eng.simulate_torch(d_true)
     d_start = torch.from_numpy(start).to(dev)
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         eng.evaluate_adjoint_torch(d_start, d_obs)
     torch.cuda.synchronize()
     stop = threading.Event()
@@ -346,7 +346,7 @@ def run_large(args):
     _lib.launch_count(reset=True)
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     ev0.record()
-    for _ in range(args.steps):
+    for _ in range(steps):
         loss, grad = eng.evaluate_adjoint_torch(d_start, d_obs, check_status=False)
     ev1.record()
     torch.cuda.synchronize()
@@ -360,7 +360,20 @@ def run_large(args):
     assert torch.isfinite(loss).all() and torch.isfinite(grad).all()
     upd = (eng.nx - 4) * (eng.nz - 4)
     cell_updates = 2.0 * upd * nt * shots  # forward + adjoint per gradient
-    value = cell_updates * args.steps / (ms / 1000.0) / 1e9
+    value = cell_updates * steps / (ms / 1000.0) / 1e9
+    # simulate alone (forward only), one step per launch and temporally blocked (4 steps per launch)
+    sim_ms = {}
+    for tb in (0, 1):
+        eng.set_option("temporal_block", tb)
+        eng.simulate_torch(d_true, check_status=False)  # first use allocates the blocked kernels' state
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        eng.simulate_torch(d_true, check_status=False)
+        e1.record()
+        torch.cuda.synchronize()
+        eng.status("simulate")
+        sim_ms[tb] = e0.elapsed_time(e1)
+    eng.set_option("temporal_block", 0)
     # e2e: host velocity and observed data in, loss and gradient out, through the C ABI host entry
     h_vel = torch.from_numpy(start).pin_memory()
     h_obs = d_obs.cpu().pin_memory()
@@ -374,38 +387,53 @@ def run_large(args):
 
     host_step()
     t0 = time.perf_counter()
-    for _ in range(args.steps):
+    for _ in range(steps):
         host_step()
     e2e_s = time.perf_counter() - t0
-    e2e = cell_updates * args.steps / e2e_s / 1e9
+    e2e = cell_updates * steps / e2e_s / 1e9
     bf, ba = large_bytes_per_cell_update(eng.nx, eng.nz, PML, shots)
     fms, fn = prof["forward"]
     ams, an = prof["adjoint"]
-    per_launch = upd * shots  # cell-updates per step launch
-    dom, dms, dbytes = ("adjoint", ams / max(an, 1) / nt, ba) if ams >= fms else ("forward", fms / max(fn, 1) / nt, bf)
-    achieved = per_launch * dbytes / (dms / 1000.0) / 1e9
+    per_launch = upd * shots  # cell-updates per step (the adjoint runs one launch per step)
+    dms = ams / max(an, 1) / nt
+    achieved = per_launch * ba / (dms / 1000.0) / 1e9
     hbm_peak, peak_kind = measured_peaks()
-    line = {
-        "metric": LARGE_METRIC, "value": value, "unit": LARGE_UNIT, "n_gpus": 1, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+    fwd_step_ms = fms / max(fn, 1) / nt
+    eng.close()
+    return {
+        "metric": LARGE_METRIC, "value": value, "unit": LARGE_UNIT, "n_gpus": 1, "steps": steps,
+        "warmup": warmup, "ms_per_step": ms / steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded faulted layered model, smoothed start)",
         "config": {"workload": f"large survey: 800x300 cells at 5 m (padded 844x344), {shots} shots, "
                                f"800 receivers, dt=0.5ms, nt={nt}, forward + exact adjoint gradient, streamed path",
                    "checkpointing": "every step's gradient term stored in HBM when it fits (auto)",
+                   "temporal_block": "off (one step per launch); `simulate` also times the engine option",
                    "l2": "inputs larger than L2 (wavefields ~93 MB + stored terms ~186 GB per gradient)"},
-        "gradients_per_s": args.steps / (ms / 1000.0),
+        "gradients_per_s": steps / (ms / 1000.0),
+        "simulate": {f"temporal_block_{tb}": {"ms": t, "gcell_updates_per_s": upd * nt * shots / (t / 1000.0) / 1e9}
+                     for tb, t in sim_ms.items()},
         "e2e": {"value": e2e, "unit": LARGE_UNIT, "h2d_bytes_per_step": h_vel.numel() * 4 + h_obs.numel() * 4,
                 "d2h_bytes_per_step": 8 + h_grad.numel() * 4},
         "gpu_launches": launches,
-        "kernels_ms": {"forward": {"total_ms": fms, "steps": nt * max(fn, 1)},
-                       "adjoint": {"total_ms": ams, "steps": nt * max(an, 1)}},
-        "roofline": {"kernel": f"{dom} step", "bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+        "kernels_ms": {"forward": {"total_ms": fms, "steps": nt * max(fn, 1), "ms_per_step": fwd_step_ms},
+                       "adjoint": {"total_ms": ams, "steps": nt * max(an, 1), "ms_per_step": dms}},
+        "roofline": {"kernel": "adjoint step", "bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                      "frac": achieved / hbm_peak, "peak_source": peak_kind, "traffic": None,
-                     "bytes_per_cell_update": {"forward": bf, "adjoint": ba}, "avg_launch_ms": dms,
-                     "bytes_per_launch": per_launch * dbytes},
+                     "bytes_per_cell_update": {"forward_per_step_kernel": bf, "adjoint": ba},
+                     "avg_launch_ms": dms, "bytes_per_launch": per_launch * ba,
+                     "forward_fp32": {"ms_per_step": fwd_step_ms,
+                                      "gcell_updates_per_s": per_launch / (fwd_step_ms / 1000.0) / 1e9}},
         "clocks": summarize_clocks(clk),
     }
+
+
+def run_large(args):
+    import torch
+
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    line = measure_large(args.nt, args.shots, args.steps, args.warmup)
     if not args.no_cpu_baseline:
+        true, start = large_workload(args.nt, args.shots)
         v, cores, sample = large_cpu_rate(true, start)
         line["cpu_baseline"] = {"value": v, "unit": LARGE_UNIT, "cores": cores, "kind": "port", "sample": sample}
     print(json.dumps(line), flush=True)
@@ -627,6 +655,8 @@ def main():
     ap.add_argument("--nt", type=int, default=NT, help="time steps (profiling runs use a short record)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-autotune", action="store_true", help="keep the engine's default launch shapes")
+    ap.add_argument("--no-large", action="store_true",
+                    help="skip the short measurement of the 800x300 streamed survey in the default run")
     ap.add_argument("--no-fast", action="store_true",
                     help="skip the secondary measurement with the fast-arithmetic forward (arith 1)")
     ap.add_argument("--arith", default="exact", choices=["exact", "fast"],
@@ -808,6 +838,12 @@ def main():
         v, secs = cpu_baseline(start, d_obs[: 2 * cores].cpu().numpy(), src, cores, 2 * cores)
         line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
                                 "sample": f"{2 * cores} of the {M} gradients ({secs:.1f} s), one model per thread"}
+    if not args.no_large and rank == 0 and world == 1:
+        # the large streamed survey, briefly: its own line is `--workload large`
+        eng.close()
+        del d_obs, d_start, d_true, h_obs
+        torch.cuda.empty_cache()
+        line["large_survey"] = measure_large(4000, 40, steps=2, warmup=1)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if dist:

@@ -103,7 +103,11 @@ int wg_get_checkpoint_interval(const wg_engine* eng);
  * kernels compute the same discrete operator with 1/h folded into the stencil weights and fused
  * multiply-adds, faster and equal to f32 accuracy, on the resident kernels of the default 70x70,
  * 100x100 and 140x140 shapes; the adjoint, other shapes and the streamed path keep the unfused
- * arithmetic). No reference counterpart. */
+ * arithmetic), "temporal_block" (0/1, default 0; 1: on the streamed path, forward passes that
+ * start from the zero state and need no checkpoints (simulate, and the gradient's forward when
+ * every step's gradient term is kept) advance each tile 4 steps per launch from a halo of 8 cells
+ * held in shared memory, with identical results; slower than the per-step kernels on the 800x300
+ * survey, whose per-step forward is not bandwidth-bound). No reference counterpart. */
 int wg_set_option(wg_engine* eng, const char* key, int value);
 int wg_get_option(const wg_engine* eng, const char* key, int* value);
 

@@ -123,3 +123,28 @@ def test_streamed_option_errors(cuda_lib):
     big = _engine(o.Survey(shots=1, nt=20, dt=0.0005, h=5.0, nx_vis=800, nz_vis=300), streamed=None)
     with pytest.raises(Exception):
         big.set_option("streamed", 0)
+
+
+def test_temporal_blocking_equals_the_per_step_kernels(cuda_lib):
+    """The temporally blocked forward (4 steps per launch from an 8-cell halo) against the per-step
+    streamed kernels and the oracle, bit for bit: nt not a multiple of 4 (a short last launch),
+    4 x 5 tiles, a source whose corners straddle a tile corner (its halo copies must be injected)
+    and one deep in the grid; simulate and the store-every-step gradient."""
+    sv = o.Survey(shots=4, nt=203, dt=0.0005, h=5.0, nx_vis=152, nz_vis=90, pml=20)  # padded 196 x 134
+    eng = _engine(sv)
+    assert eng.get_option("temporal_block") == 0
+    # padded x 64 / z 32 are tile boundaries: (41.5 + 22, 9.5 + 22) puts the corners on both sides
+    src = np.array([[207.5, 47.5], [0.0, 5.0], [512.5, 7.5], [637.5, 352.5]], np.float32)
+    eng.set_sources(src)
+    vel = _models(sv, 2, 5)
+    obs = o.forward(sv, vel * np.float32(1.03), src, eng.wavelet())
+    eng.checkpoint_every = 0
+    eng.set_option("temporal_block", 0)
+    ref_sim = eng.simulate(vel)
+    ref_loss, ref_grad = eng.evaluate_adjoint(vel, obs)
+    eng.set_option("temporal_block", 1)
+    np.testing.assert_array_equal(eng.simulate(vel), ref_sim)
+    np.testing.assert_array_equal(ref_sim, o.forward(sv, vel, src, eng.wavelet()))
+    loss, grad = eng.evaluate_adjoint(vel, obs)
+    np.testing.assert_array_equal(grad, ref_grad)
+    np.testing.assert_array_equal(loss, ref_loss)

@@ -146,6 +146,7 @@ struct wg_engine {
   int ck_every = 50;
   int adj_prefetch = 1;
   int fast = 0;      // 1: fast-arithmetic resident kernels (option "arith")
+  int tblock = 0;    // streamed path: temporally blocked forward (option "temporal_block")
   int streamed = 0;  // 1: wavefields in HBM, one launch per step (grids beyond the resident kernels)
   cudaStream_t copy_stream = nullptr;  // host->device copy of observed data, overlapping the forward
   cudaEvent_t obs_ready = nullptr;
@@ -216,6 +217,7 @@ wg::EngineView view_of(const wg_engine* e) {
   v.d_status = e->d_status.as<int>();
   v.adj_prefetch = e->adj_prefetch;
   v.fast = e->fast;
+  v.tblock = e->tblock;
   return v;
 }
 
@@ -876,6 +878,8 @@ int wg_set_option(wg_engine* e, const char* key, int value) {
   } else if (k == "arith") {
     if (value != 0 && value != 1) return fail(WG_ERR_ARG, "arith must be 0 (reference order) or 1 (fast)");
     e->fast = value;
+  } else if (k == "temporal_block") {
+    e->tblock = value ? 1 : 0;
   } else if (k == "streamed") {
     if (value) {
       std::string why;
@@ -899,6 +903,8 @@ int wg_get_option(const wg_engine* e, const char* key, int* value) {
     *value = e->adj_prefetch;
   } else if (k == "arith") {
     *value = e->fast;
+  } else if (k == "temporal_block") {
+    *value = e->tblock;
   } else if (k == "streamed") {
     *value = e->streamed;
   } else {

@@ -410,6 +410,285 @@ __global__ void __launch_bounds__(FWD_THREADS, 2) fwd_stream_kernel(const __grid
 }
 
 // ------------------------------------------------------------------------------------------------
+// Temporally blocked forward: TB_T steps per launch. Each job (unit, 64 x 32 tile) takes its tile
+// with a halo of 2 TB_T cells per side (the stencil reaches 2 cells per step) into shared memory:
+// u(t), u(t-1) and the velocity by TMA (double-buffered: the next job's boxes land while this one
+// computes), and, on tiles that reach a C-PML strip, a*psi and zeta of the strip cells. It then
+// advances the region TB_T steps in shared memory, the computed region shrinking by 2 cells per
+// side per step, and writes back the tile: the halo cells are computed by every tile that holds
+// them, with the same operations on the same values, so each cell's value is the per-step kernel's
+// bit for bit (sources are injected into halo copies too; receivers are recorded by the tile that
+// holds their first corner). Per step the wavefield crosses HBM once per TB_T steps instead of once
+// per step. The state is read from one set and written to the other (sets alternate per launch),
+// so no CTA overwrites cells a neighbouring CTA still has to read.
+// ------------------------------------------------------------------------------------------------
+constexpr int TB_T = 4;                      // time steps per launch
+constexpr int TB_H = 2 * TB_T;               // halo per side
+constexpr int TB_RX = TX_ + 2 * TB_H;        // 80 region columns (x offset 64 k - 8: 16-byte aligned)
+constexpr int TB_RZ = TZ_ + 2 * TB_H;        // 48 region rows
+constexpr int TB_N = TB_RX * TB_RZ;          // cells of a region
+constexpr int TB_THREADS = 512;
+constexpr int TB_STAGE = 3 * TB_N;           // floats per stage: u(t) | u(t-1) | v
+constexpr size_t kTbSmem = static_cast<size_t>(2 * TB_STAGE + 6 * TB_N) * 4 + 2 * 8 + 128;
+
+struct TbArgs {
+  SArgs a;         // geometry, stations, profiles, traces, stored terms, status; a.t = first step
+  int nsub;        // steps of this launch, 1..TB_T
+  int set_in;      // state set read (the other one is written)
+  float* W;        // [2 sets][2 levels: u(t), u(t-1)][units][nz][nx]
+  float* PX;       // a psi_x [2 sets][units][nz][2 ssw]
+  float* ZX;       // zeta_x  [2 sets][units][nz][2 ssw]
+  float* PZ;       // a psi_z [2 sets][units][2 ssw][nx]
+  float* ZZ;       // zeta_z  [2 sets][units][2 ssw][nx]
+};
+
+template <bool TRACES, bool STORE>
+__global__ void __launch_bounds__(TB_THREADS, 1) fwd_tb_kernel(const __grid_constant__ CUtensorMap umap,
+                                                               const __grid_constant__ CUtensorMap vmap,
+                                                               const __grid_constant__ TbArgs p) {
+  extern __shared__ __align__(128) float tsm_raw[];
+  float* sm = tsm_raw + ((128 - (smem_u32(tsm_raw) & 127)) & 127) / 4;
+  float* stages = sm;             // [2][u(t) | u(t-1) | v]
+  float* PXA = sm + 2 * TB_STAGE;  // a psi_x, two buffers (neighbours read x +- 2)
+  float* PXB = PXA + TB_N;
+  float* ZXr = PXB + TB_N;         // zeta_x (owner only, updated in place)
+  float* PZA = ZXr + TB_N;         // a psi_z, two buffers
+  float* PZB = PZA + TB_N;
+  float* ZZr = PZB + TB_N;
+  uint64_t* full = reinterpret_cast<uint64_t*>(ZZr + TB_N);
+  const SArgs& a = p.a;
+  const int tid = threadIdx.x;
+  const int tiles = a.tiles_x * a.tiles_z;
+  const int jobs = a.units * tiles;
+  const int nx = a.nx, nz = a.nz, ssw = a.ssw, region = a.region;
+  const size_t cells = static_cast<size_t>(nx) * nz;
+  const size_t xs_unit = static_cast<size_t>(nz) * 2 * ssw, zs_unit = static_cast<size_t>(2) * ssw * nx;
+  const int set_out = 1 - p.set_in;
+  if (tid == 0) {
+    mbar_init(&full[0], 1);
+    mbar_init(&full[1], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  auto issue = [&](int job, int s) {
+    const int unit = job / tiles, tile = job % tiles;
+    const int x = (tile % a.tiles_x) * TX_ - TB_H, z = (tile / a.tiles_x) * TZ_ - TB_H;
+    float* st = stages + s * TB_STAGE;
+    mbar_expect_tx(&full[s], TB_STAGE * 4);
+    tma_load(st, &umap, x, z, (p.set_in * 2 + 0) * a.units + unit, &full[s]);
+    tma_load(st + TB_N, &umap, x, z, (p.set_in * 2 + 1) * a.units + unit, &full[s]);
+    tma_load(st + 2 * TB_N, &vmap, x, z, unit / a.shots, &full[s]);
+  };
+  if (tid == 0 && static_cast<int>(blockIdx.x) < jobs) issue(blockIdx.x, 0);
+  int i = 0;
+  for (int job = blockIdx.x; job < jobs; job += gridDim.x, ++i) {
+    const int s = i & 1;
+    const bool next = job + static_cast<int>(gridDim.x) < jobs;
+    if (tid == 0 && next) {  // the other stage's last job ended with a CTA barrier
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      issue(job + gridDim.x, 1 - s);
+    }
+    const bool ok = mbar_wait(&full[s], (i >> 1) & 1);
+    if (__syncthreads_or(!ok)) {
+      if (tid == 0) {
+        report(a.status);
+        if (next) mbar_wait(&full[1 - s], ((i + 1) >> 1) & 1);  // the copies still landing (bounded)
+      }
+      return;
+    }
+    const int unit = job / tiles, tile = job % tiles;
+    const int x0 = (tile % a.tiles_x) * TX_, z0 = (tile / a.tiles_x) * TZ_;
+    const int rx0 = x0 - TB_H, rz0 = z0 - TB_H;  // region origin in grid coordinates
+    const int shot = unit % a.shots;
+    float* U = stages + s * TB_STAGE;
+    float* UP = U + TB_N;
+    const float* V = UP + TB_N;
+    const bool pml_tile = rx0 < ssw || rx0 + TB_RX > nx - ssw || rz0 < ssw || rz0 + TB_RZ > nz - ssw;
+    if (pml_tile) {
+      const float* PXi = p.PX + (static_cast<size_t>(p.set_in) * a.units + unit) * xs_unit;
+      const float* ZXi = p.ZX + (static_cast<size_t>(p.set_in) * a.units + unit) * xs_unit;
+      const float* PZi = p.PZ + (static_cast<size_t>(p.set_in) * a.units + unit) * zs_unit;
+      const float* ZZi = p.ZZ + (static_cast<size_t>(p.set_in) * a.units + unit) * zs_unit;
+      for (int c = tid; c < TB_N; c += TB_THREADS) {
+        const int z = rz0 + c / TB_RX, x = rx0 + c % TB_RX;
+        float px = 0.f, zx = 0.f, pz = 0.f, zz = 0.f;
+        if (x >= 0 && x < nx && z >= 0 && z < nz) {
+          if (x < ssw || x >= nx - ssw) {
+            const int k = z * 2 * ssw + xstrip(x, nx, ssw);
+            px = PXi[k];
+            zx = ZXi[k];
+          }
+          if (z < ssw || z >= nz - ssw) {
+            const int k = (z < ssw ? z : z - (nz - 2 * ssw)) * nx + x;
+            pz = PZi[k];
+            zz = ZZi[k];
+          }
+        }
+        // both buffers: a*psi of strip cells outside the C-PML region is never updated
+        PXA[c] = px;
+        PXB[c] = px;
+        ZXr[c] = zx;
+        PZA[c] = pz;
+        PZB[c] = pz;
+        ZZr[c] = zz;
+      }
+      __syncthreads();
+    }
+    const int* sc = a.st.src_cell + 4 * shot;
+    const float* sw = a.st.src_w + 4 * shot;
+    const int sc0 = __ldg(&sc[0]), sc1 = __ldg(&sc[1]), sc2 = __ldg(&sc[2]), sc3 = __ldg(&sc[3]);
+    for (int k = 0; k < p.nsub; ++k) {
+      const int t = a.t + k;
+      const float f = __ldg(&a.wavelet[t]);
+      const float* Uc = (k & 1) ? UP : U;  // u(t)
+      float* Un = (k & 1) ? U : UP;        // u(t - 1), overwritten by u(t + 1)
+      const float* Pc = (k & 1) ? PXB : PXA;
+      float* Pn = (k & 1) ? PXA : PXB;
+      const float* Qc = (k & 1) ? PZB : PZA;
+      float* Qn = (k & 1) ? PZA : PZB;
+      if (TRACES) {
+        const int r0 = a.tile_rec_start[tile], r1 = a.tile_rec_start[tile + 1];
+        for (int q = r0 + tid; q < r1; q += TB_THREADS) {
+          const int r = a.tile_rec[q];
+          float acc = 0.0f;
+#pragma unroll
+          for (int cc = 0; cc < 4; ++cc) {
+            const int cell = a.st.rec_cell[4 * r + cc];
+            acc = acc + a.st.rec_w[4 * r + cc] * Uc[(cell / nx - rz0) * TB_RX + (cell % nx - rx0)];
+          }
+          a.traces[(static_cast<size_t>(unit) * a.nt + t) * a.st.nrec + r] = acc;
+        }
+      }
+      float* stp = STORE ? a.stored + (static_cast<size_t>(unit) * a.seg + (t - a.seg_t0)) * cells : nullptr;
+      const int m = 2 * (k + 1);  // region of step k: 2 (k + 1) cells inside the loaded one
+      const int pairs = (TB_RX - 2 * m) / 2, rows = TB_RZ - 2 * m;
+      for (int idx = tid; idx < pairs * rows; idx += TB_THREADS) {
+        const int lz = m + idx / pairs, lx = m + 2 * (idx % pairs);
+        const int z = rz0 + lz, x = rx0 + lx;
+        if (z < FD_PAD || z >= nz - FD_PAD || x < FD_PAD || x + 1 >= nx - FD_PAD) continue;
+        const int c = lz * TB_RX + lx;
+        const int cell = z * nx + x;
+        const float2 U0 = lds2(Uc + c);
+        const float2 A = lds2(Uc + c - 2);
+        const float2 B = lds2(Uc + c + 2);
+        const float u0 = U0.x, u1 = U0.y;
+        const float d2x0 = (((F_D2A * u0 + F_D2B * (u1 + A.y)) - F_D2C * (B.x + A.x)) * a.d2a) * a.d2b;
+        const float d2x1 = (((F_D2A * u1 + F_D2B * (B.x + u0)) - F_D2C * (B.y + A.y)) * a.d2a) * a.d2b;
+        float w0, w1;
+        if (x < region || x + 1 >= nx - region) {
+          const float2 pa = ldg2(a.prof + x), pb = ldg2(a.prof + nx + x), pd = ldg2(a.prof + 2 * nx + x);
+          const float ax0 = pa.x, ax1 = pa.y, bx0 = pb.x, bx1 = pb.y, dbx0 = pd.x, dbx1 = pd.y;
+          const float opbx0 = 1.0f + bx0, opbx1 = 1.0f + bx1;
+          const float2 P0 = lds2(Pc + c - 2), P1 = lds2(Pc + c), P2 = lds2(Pc + c + 2);
+          const float2 Z = lds2(ZXr + c);
+          const float d10 = ((F_D1A * (u1 - A.y)) - F_D1B * (B.x - A.x)) * a.rh;
+          const float d11 = ((F_D1A * (B.x - u0)) - F_D1B * (B.y - A.y)) * a.rh;
+          const float da0 = ((F_D1A * (P1.y - P0.y)) - F_D1B * (P2.x - P0.x)) * a.rh;
+          const float da1 = ((F_D1A * (P2.x - P1.x)) - F_D1B * (P2.y - P0.y)) * a.rh;
+          const float tmp0 = ((opbx0 * d2x0) + (dbx0 * d10)) + da0;
+          const float tmp1 = ((opbx1 * d2x1) + (dbx1 * d11)) + da1;
+          w0 = (opbx0 * tmp0) + (ax0 * Z.x);
+          w1 = (opbx1 * tmp1) + (ax1 * Z.y);
+          const float psi0 = (bx0 * d10) + P1.x;
+          const float psi1 = (bx1 * d11) + P1.y;
+          st2(ZXr + c, (bx0 * tmp0) + (ax0 * Z.x), (bx1 * tmp1) + (ax1 * Z.y));
+          st2(Pn + c, ax0 * psi0, ax1 * psi1);
+        } else {
+          w0 = d2x0;
+          w1 = d2x1;
+        }
+        const float2 zm2 = lds2(Uc + c - 2 * TB_RX), zm1 = lds2(Uc + c - TB_RX), zp1 = lds2(Uc + c + TB_RX),
+                     zp2 = lds2(Uc + c + 2 * TB_RX);
+        const float d2z0 = (((F_D2A * u0 + F_D2B * (zp1.x + zm1.x)) - F_D2C * (zp2.x + zm2.x)) * a.d2a) * a.d2b;
+        const float d2z1 = (((F_D2A * u1 + F_D2B * (zp1.y + zm1.y)) - F_D2C * (zp2.y + zm2.y)) * a.d2a) * a.d2b;
+        if (z < region || z >= nz - region) {
+          const float az = __ldg(&a.prof[3 * nx + z]), bz = __ldg(&a.prof[3 * nx + nz + z]),
+                      dbz = __ldg(&a.prof[3 * nx + 2 * nz + z]);
+          const float opbz = 1.0f + bz;
+          const float2 Qm2 = lds2(Qc + c - 2 * TB_RX), Qm1 = lds2(Qc + c - TB_RX), Q0 = lds2(Qc + c),
+                       Qp1 = lds2(Qc + c + TB_RX), Qp2 = lds2(Qc + c + 2 * TB_RX);
+          const float2 Z = lds2(ZZr + c);
+          const float d10 = ((F_D1A * (zp1.x - zm1.x)) - F_D1B * (zp2.x - zm2.x)) * a.rh;
+          const float d11 = ((F_D1A * (zp1.y - zm1.y)) - F_D1B * (zp2.y - zm2.y)) * a.rh;
+          const float da0 = ((F_D1A * (Qp1.x - Qm1.x)) - F_D1B * (Qp2.x - Qm2.x)) * a.rh;
+          const float da1 = ((F_D1A * (Qp1.y - Qm1.y)) - F_D1B * (Qp2.y - Qm2.y)) * a.rh;
+          const float tmp0 = ((opbz * d2z0) + (dbz * d10)) + da0;
+          const float tmp1 = ((opbz * d2z1) + (dbz * d11)) + da1;
+          w0 = w0 + ((opbz * tmp0) + (az * Z.x));
+          w1 = w1 + ((opbz * tmp1) + (az * Z.y));
+          const float psi0 = (bz * d10) + Q0.x;
+          const float psi1 = (bz * d11) + Q0.y;
+          st2(ZZr + c, (bz * tmp0) + (az * Z.x), (bz * tmp1) + (az * Z.y));
+          st2(Qn + c, az * psi0, az * psi1);
+        } else {
+          w0 = w0 + d2z0;
+          w1 = w1 + d2z1;
+        }
+        const float2 v = lds2(V + c);
+        const float v20 = (v.x * v.x) * a.dt2, v21 = (v.y * v.y) * a.dt2;
+        const float2 prev = lds2(Un + c);
+        float n0 = ((v20 * w0) + (2.0f * u0)) - prev.x;
+        float n1 = ((v21 * w1) + (2.0f * u1)) - prev.y;
+        if (STORE && lz >= TB_H && lz < TB_H + TZ_ && lx >= TB_H && lx < TB_H + TX_)
+          __stcs(reinterpret_cast<float2*>(stp + cell),
+                 make_float2(((2.0f * v.x) * a.dt2) * w0, ((2.0f * v.y) * a.dt2) * w1));
+        // sources: corners in the halo are injected too, so that halo copies match their owners
+        if (cell == sc0 || cell + 1 == sc0 || cell == sc1 || cell + 1 == sc1 || cell == sc2 || cell + 1 == sc2 ||
+            cell == sc3 || cell + 1 == sc3) {
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            const int scq = q == 0 ? sc0 : q == 1 ? sc1 : q == 2 ? sc2 : sc3;
+            if (cell == scq) n0 = n0 + (((-v20) * __ldg(&sw[q])) * f);
+            if (cell + 1 == scq) n1 = n1 + (((-v21) * __ldg(&sw[q])) * f);
+          }
+        }
+        st2(Un + c, n0, n1);
+      }
+      __syncthreads();
+    }
+    // write back the tile: u(t + nsub), u(t + nsub - 1), and the strip cells' C-PML state
+    const int ns = p.nsub;
+    const float* Ucur = (ns & 1) ? UP : U;
+    const float* Uold = (ns & 1) ? U : UP;
+    float* W0 = p.W + (static_cast<size_t>(set_out * 2 + 0) * a.units + unit) * cells;
+    float* W1 = p.W + (static_cast<size_t>(set_out * 2 + 1) * a.units + unit) * cells;
+    for (int idx = tid; idx < TZ_ * (TX_ / 4); idx += TB_THREADS) {
+      const int lz = idx / (TX_ / 4), lx4 = 4 * (idx % (TX_ / 4));
+      const int z = z0 + lz, x = x0 + lx4;
+      if (z >= nz || x >= nx) continue;  // nx is a multiple of 4
+      const int c = (lz + TB_H) * TB_RX + lx4 + TB_H;
+      *reinterpret_cast<float4*>(W0 + z * nx + x) = *reinterpret_cast<const float4*>(Ucur + c);
+      *reinterpret_cast<float4*>(W1 + z * nx + x) = *reinterpret_cast<const float4*>(Uold + c);
+    }
+    if (pml_tile) {
+      const float* Pcur = (ns & 1) ? PXB : PXA;
+      const float* Qcur = (ns & 1) ? PZB : PZA;
+      float* PXo = p.PX + (static_cast<size_t>(set_out) * a.units + unit) * xs_unit;
+      float* ZXo = p.ZX + (static_cast<size_t>(set_out) * a.units + unit) * xs_unit;
+      float* PZo = p.PZ + (static_cast<size_t>(set_out) * a.units + unit) * zs_unit;
+      float* ZZo = p.ZZ + (static_cast<size_t>(set_out) * a.units + unit) * zs_unit;
+      for (int idx = tid; idx < TZ_ * TX_; idx += TB_THREADS) {
+        const int lz = idx / TX_, lx = idx % TX_;
+        const int z = z0 + lz, x = x0 + lx;
+        if (z >= nz || x >= nx) continue;
+        const int c = (lz + TB_H) * TB_RX + lx + TB_H;
+        if (x < ssw || x >= nx - ssw) {
+          const int k = z * 2 * ssw + xstrip(x, nx, ssw);
+          PXo[k] = Pcur[c];
+          ZXo[k] = ZXr[c];
+        }
+        if (z < ssw || z >= nz - ssw) {
+          const int k = (z < ssw ? z : z - (nz - 2 * ssw)) * nx + x;
+          PZo[k] = Qcur[c];
+          ZZo[k] = ZZr[c];
+        }
+      }
+    }
+    __syncthreads();  // this stage and the C-PML arrays are free again
+  }
+}
+
+// ------------------------------------------------------------------------------------------------
 // Adjoint step t (reverse time): lambda_next = w + 2 lambda - lambda_prev + injected residuals,
 // gradient += lambda * stored term (+ the source-term correction), splatAdjoint.wgsl:58-131.
 // Derived terms v^2 dt^2 lambda (VS) and, in the PML strips, T = (1+b) VS + b zeta and
@@ -770,10 +1049,11 @@ constexpr size_t kAdjSmem = (7 * BZ * BX) * 4 + 16 + 128;
 struct StreamWork {
   Buf vpad, mask, traces, energy, scale, stored, ckpt, gacc;
   Buf W, PX, ZX, PZ, ZZ;        // forward state
+  Buf Wtb, PXtb, ZXtb, PZtb, ZZtb;  // temporally blocked forward: two state sets
   Buf L, LPX, LZX, LPZ, LZZ;    // adjoint state
   Buf tile_rec_start, tile_rec;
   int rec_tiles_nx = -1, rec_tiles_nz = -1, rec_z0 = 0, rec_z1 = -1;
-  int fwd_blocks = 0, adj_blocks = 0, sms = 0;
+  int fwd_blocks = 0, adj_blocks = 0, tb_blocks = 0, sms = 0;
 };
 
 StreamWork* stream_work_new() { return new StreamWork(); }
@@ -837,11 +1117,18 @@ int occupancy(StreamWork* w) {
                              static_cast<int>(kFwdSmem)));
   SW_CK(cudaFuncSetAttribute(fwd_stream_kernel<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              static_cast<int>(kFwdSmem)));
+  SW_CK(cudaFuncSetAttribute(fwd_tb_kernel<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             static_cast<int>(kTbSmem)));
+  SW_CK(cudaFuncSetAttribute(fwd_tb_kernel<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             static_cast<int>(kTbSmem)));
   SW_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fb, fwd_stream_kernel<true, true>, FWD_THREADS, kFwdSmem));
   SW_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ab, adj_stream_kernel, NTH, kAdjSmem));
+  int tb = 0;
+  SW_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&tb, fwd_tb_kernel<true, true>, TB_THREADS, kTbSmem));
   w->sms = sms;
   w->fwd_blocks = sms * std::max(fb, 1);
   w->adj_blocks = sms * std::max(ab, 1);
+  w->tb_blocks = sms * std::max(tb, 1);
   return WG_OK;
 }
 
@@ -916,6 +1203,54 @@ int adj_step(StreamWork* w, const CUtensorMap& map, SArgs a, int t, cudaStream_t
   return WG_OK;
 }
 
+// Temporally blocked forward over all units from the zero state, TB_T steps per launch: receivers
+// into `traces` and, when `stored` is given, every step's gradient term (the store-all scheme).
+int tb_forward(StreamWork* w, const EngineView& v, int units, int models, float* traces, float* stored,
+               cudaStream_t st) {
+  const size_t cells = static_cast<size_t>(v.nx) * v.nz;
+  const size_t nW = static_cast<size_t>(units) * cells, nX = units * xs_floats(v), nZ = units * zs_floats(v);
+  SW_CK(w->Wtb.ensure(4 * nW * 4));
+  SW_CK(w->PXtb.ensure(2 * nX * 4));
+  SW_CK(w->ZXtb.ensure(2 * nX * 4));
+  SW_CK(w->PZtb.ensure(2 * nZ * 4));
+  SW_CK(w->ZZtb.ensure(2 * nZ * 4));
+  SW_CK(cudaMemsetAsync(w->Wtb.p, 0, 4 * nW * 4, st));
+  SW_CK(cudaMemsetAsync(w->PXtb.p, 0, 2 * nX * 4, st));
+  SW_CK(cudaMemsetAsync(w->ZXtb.p, 0, 2 * nX * 4, st));
+  SW_CK(cudaMemsetAsync(w->PZtb.p, 0, 2 * nZ * 4, st));
+  SW_CK(cudaMemsetAsync(w->ZZtb.p, 0, 2 * nZ * 4, st));
+  CUtensorMap um, vm;
+  int rc = make_map(&um, w->Wtb.f(), v.nx, v.nz, 4 * units, TB_RX, TB_RZ);
+  if (rc == WG_OK) rc = make_map(&vm, w->vpad.f(), v.nx, v.nz, models, TB_RX, TB_RZ);
+  if (rc != WG_OK) return rc;
+  TbArgs p{};
+  p.a = base_args(w, v, units);
+  p.a.vel = w->vpad.f();
+  p.a.traces = traces;
+  p.a.stored = stored;
+  p.a.seg = v.nt;
+  p.a.seg_t0 = 0;
+  p.W = w->Wtb.f();
+  p.PX = w->PXtb.f();
+  p.ZX = w->ZXtb.f();
+  p.PZ = w->PZtb.f();
+  p.ZZ = w->ZZtb.f();
+  const int jobs = units * p.a.tiles_x * p.a.tiles_z;
+  const int blocks = std::min(jobs, w->tb_blocks);
+  for (int t = 0, k = 0; t < v.nt; t += TB_T, ++k) {
+    p.a.t = t;
+    p.nsub = std::min(TB_T, v.nt - t);
+    p.set_in = k & 1;
+    note_launch();
+    if (stored)
+      fwd_tb_kernel<true, true><<<blocks, TB_THREADS, kTbSmem, st>>>(um, vm, p);
+    else
+      fwd_tb_kernel<true, false><<<blocks, TB_THREADS, kTbSmem, st>>>(um, vm, p);
+    SW_CK(cudaGetLastError());
+  }
+  return WG_OK;
+}
+
 // Checkpoint slot layout: [W(t) | W(t-1) | PX(t) | ZX | PZ(t) | ZZ] for all units.
 size_t ckpt_slot_floats(const EngineView& v, int units) {
   const size_t cells = static_cast<size_t>(v.nx) * v.nz;
@@ -966,6 +1301,12 @@ int stream_simulate(StreamWork* w, const EngineView& v, const int* h_rec_cell, c
   SW_CK(w->vpad.ensure(models * cells * 4));
   note_launch();
   SW_CK(launch_pad_velocity(d_vis, models, v.nx_vis, v.nz_vis, v.pad, v.vmin, v.vmax, w->vpad.f(), nullptr, st));
+  if (v.tblock) {
+    timer.mark(0, true, st);
+    if ((rc = tb_forward(w, v, units, models, d_traces, nullptr, st)) != WG_OK) return rc;
+    timer.mark(0, false, st);
+    return WG_OK;
+  }
   if ((rc = alloc_forward(w, v, units, st)) != WG_OK) return rc;
   FwdMaps map;
   if ((rc = make_fwd_maps(&map, w->W.f(), w->vpad.f(), v.nx, v.nz, units, models)) != WG_OK) return rc;
@@ -1056,10 +1397,15 @@ int stream_gradient(StreamWork* w, const EngineView& v, const int* h_rec_cell, c
   f.seg = seg;
   f.seg_t0 = 0;
   timer.mark(0, true, st);
-  for (int t = 0; t < v.nt; ++t) {
-    if (!store_all && t > 0 && t % k == 0)
-      if ((rc = ckpt_copy(w, v, units, t, w->ckpt.f() + (t / k - 1) * (slot_bytes / 4), true, st)) != WG_OK) return rc;
-    if ((rc = fwd_step(w, fmap, f, t, true, store_all, st)) != WG_OK) return rc;
+  if (store_all && v.tblock) {
+    if ((rc = tb_forward(w, v, units, models, w->traces.f(), w->stored.f(), st)) != WG_OK) return rc;
+  } else {
+    for (int t = 0; t < v.nt; ++t) {
+      if (!store_all && t > 0 && t % k == 0)
+        if ((rc = ckpt_copy(w, v, units, t, w->ckpt.f() + (t / k - 1) * (slot_bytes / 4), true, st)) != WG_OK)
+          return rc;
+      if ((rc = fwd_step(w, fmap, f, t, true, store_all, st)) != WG_OK) return rc;
+    }
   }
   timer.mark(0, false, st);
   note_launch();

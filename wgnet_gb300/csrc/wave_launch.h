@@ -83,7 +83,8 @@ struct EngineView {
   Shape fshape, ashape;
   int* d_status;
   int adj_prefetch;
-  int fast;  // fast-arithmetic kernels (engine option "arith")
+  int fast;    // fast-arithmetic kernels (engine option "arith")
+  int tblock;  // streamed path: temporally blocked forward where it applies (engine option "temporal_block")
 };
 
 // Event marks around groups of launches (kind 0 forward, 1 forward recompute, 2 adjoint) for the

@@ -112,9 +112,12 @@ def solves_to_reach(curve: list[tuple[int, float]], target: float) -> int | None
     return None
 
 
-def evaluate(net: UpdateNet, n_models: int, seed: int, shots: int, budget: int = 160, nt: int = 1000) -> dict:
+def evaluate(net: UpdateNet, n_models: int, seed: int, shots: int, budget: int = 160, nt: int = 1000,
+             sigma: float = 5.0) -> dict:
+    """Plain and learned refinement of `n_models` held-out seeded models from a `sigma`-cell smoothed
+    start (the training trajectories start from a 5-cell smoothing)."""
     ph = physics_for(SUBSETS[shots], nt)
-    true, start, obs = problem(n_models, seed, ph)
+    true, start, obs = problem(n_models, seed, ph, sigma=sigma)
     t0 = time.perf_counter()
     plain = refine_batch(start, obs, ph, budget_solves=budget, bands_hz=BANDS, dense_block=True, true_km=true)
     t_plain = time.perf_counter() - t0
@@ -133,7 +136,7 @@ def evaluate(net: UpdateNet, n_models: int, seed: int, shots: int, budget: int =
     sp = np.array([r["solves_plain"] for r in rows], float)
     sl = np.array([r["solves_learned"] if r["solves_learned"] is not None else np.nan for r in rows], float)
     reached = np.isfinite(sl)
-    return {"shots": shots, "models": n_models, "budget": budget,
+    return {"shots": shots, "models": n_models, "budget": budget, "start_sigma_cells": sigma,
             "mae_start_km": float(np.mean([r["mae_start"] for r in rows])),
             "mae_plain_km": float(np.mean([r["mae_plain"] for r in rows])),
             "mae_learned_km": float(np.mean([r["mae_learned"] for r in rows])),
@@ -156,6 +159,9 @@ def main(argv=None) -> int:
     ap.add_argument("--out", default="learned_out")
     ap.add_argument("--weights", default=None, help="skip training: load these weights")
     ap.add_argument("--target", default="true", choices=["true", "final"])
+    ap.add_argument("--ood-models", type=int, default=0,
+                    help="also evaluate this many held-out models from a more strongly smoothed start")
+    ap.add_argument("--ood-sigma", type=float, default=8.0, help="smoothing (cells) of that start")
     args = ap.parse_args(argv)
     out = Path(args.out)
     out.mkdir(parents=True, exist_ok=True)
@@ -166,7 +172,7 @@ def main(argv=None) -> int:
         logf.write(msg + "\n")
         logf.flush()
 
-    report = {"args": vars(args)}
+    report = {"args": {k: v for k, v in vars(args).items() if k != "out"}}
     if args.weights:
         net = UpdateNet.load(args.weights)
     else:
@@ -192,6 +198,13 @@ def main(argv=None) -> int:
         r = evaluate(net, args.eval_models, seed=777, shots=shots, budget=args.eval_budget, nt=args.nt)
         log(json.dumps({k: v for k, v in r.items() if k != "per_model"}))
         report["evaluation"][str(shots)] = r
+    if args.ood_models:
+        report["evaluation_shifted_start"] = {}
+        for shots in (5, 3, 1):
+            r = evaluate(net, args.ood_models, seed=888, shots=shots, budget=args.eval_budget, nt=args.nt,
+                         sigma=args.ood_sigma)
+            log(json.dumps({k: v for k, v in r.items() if k != "per_model"}))
+            report["evaluation_shifted_start"][str(shots)] = r
     (out / "report.json").write_text(json.dumps(report, indent=1))
     return 0
 
