@@ -45,15 +45,17 @@ UPDATED_CELLS = (NX + 2 * (PML + 2) - 4) ** 2  # 110 x 110 cells updated per ste
 FLOPS_PER_CELL_UPDATE = 48.0  # average over interior / one-PML-axis / two-PML-axes cells at pml 20
 # DRAM bytes per (unit, step) measured with ncu on the small case (32 models, nt 200: the full
 # 256-model launch is too large for a multi-pass capture), scaled by unit-steps to a full launch
-MEASURED_TRAFFIC_PER_UNIT_STEP = {"adjoint": (813.03e6 + 9.72e6) / 16000, "recompute": (69.93e6 + 736.38e6) / 16000}
+MEASURED_TRAFFIC_PER_UNIT_STEP = {"adjoint": (813.12e6 + 9.30e6) / 16000, "recompute": (69.86e6 + 735.81e6) / 16000}
 # Counters of the same small-case captures (ncu --set full), per kernel: thread-instructions per
 # updated cell and step, issue slots busy, L1/shared throughput, shared-memory bank-conflict share.
 NCU_SMALL_CASE = {
-    "adjoint": {"thread_instructions_per_cell_update": None, "issue_active_pct": 60.8, "l1_shared_pct": 66.3,
-                "bank_conflict_pct_of_shared_wavefronts": 0.6},
-    "recompute": {"thread_instructions_per_cell_update": None, "issue_active_pct": 54.8, "l1_shared_pct": 56.6,
-                  "bank_conflict_pct_of_shared_wavefronts": 3.2},
+    "adjoint": {"thread_instructions_per_cell_update": 106.7, "issue_active_pct": 62.7, "l1_shared_pct": 68.0,
+                "bank_conflict_pct_of_shared_wavefronts": 1.7, "warps_active_pct": 34.3},
+    "recompute": {"thread_instructions_per_cell_update": 71.7, "issue_active_pct": 64.9, "l1_shared_pct": 52.0,
+                  "bank_conflict_pct_of_shared_wavefronts": 2.5, "warps_active_pct": 34.3},
 }
+
+
 def flops_per_cell_update(n_vis: int, pml: int = PML) -> float:
     """Algorithmic flops per updated cell and step of the forward (lib.rs:158-205; add, sub, mul 1,
     FMA 2): 24 in the interior, 54 with one C-PML axis, 84 with two, averaged over the updated
