@@ -56,16 +56,17 @@ def problem(n: int, seed: int, physics: WavePhysics, sigma: float = 5.0):
 
 
 def trajectories(n_models: int, seed: int, budget: int = 80, chunk: int = 256, nt: int = 1000,
-                 target: str = "true") -> dict:
+                 target: str = "true", sigmas: tuple[float, ...] = (5.0,)) -> dict:
     """Plain refinement trajectories; returns GPU tensors field, grad, band, target and the MAEs.
     target "true": the true model minus the recorded field (the training models are synthetic, so
-    the truth is known); "final": the trajectory's final field minus the recorded field."""
+    the truth is known); "final": the trajectory's final field minus the recorded field. The
+    starting models are the true ones smoothed by `sigmas` cells, taken in turn per chunk."""
     ph = physics_for(SUBSETS[5], nt)
     fields, grads, bands, targets = [], [], [], []
     mae0, mae1 = [], []
     for c0 in range(0, n_models, chunk):
         n = min(chunk, n_models - c0)
-        true, start, obs = problem(n, seed * 1_000_003 + c0, ph)
+        true, start, obs = problem(n, seed * 1_000_003 + c0, ph, sigma=sigmas[(c0 // chunk) % len(sigmas)])
         r = refine_batch(start, obs, ph, budget_solves=budget, bands_hz=BANDS, dense_block=True, record=True)
         final = r["final_field_km"]
         for f, g, b, rows in r["records"]:
@@ -162,6 +163,8 @@ def main(argv=None) -> int:
     ap.add_argument("--ood-models", type=int, default=0,
                     help="also evaluate this many held-out models from a more strongly smoothed start")
     ap.add_argument("--ood-sigma", type=float, default=8.0, help="smoothing (cells) of that start")
+    ap.add_argument("--train-sigmas", default="5", help="smoothing (cells) of the training starts, comma-separated, "
+                                                        "taken in turn per chunk of 256 models")
     args = ap.parse_args(argv)
     out = Path(args.out)
     out.mkdir(parents=True, exist_ok=True)
@@ -177,7 +180,9 @@ def main(argv=None) -> int:
         net = UpdateNet.load(args.weights)
     else:
         t0 = time.perf_counter()
-        data = trajectories(args.train_models, seed=1, budget=args.traj_budget, nt=args.nt, target=args.target)
+        sigmas = tuple(float(v) for v in args.train_sigmas.split(","))
+        data = trajectories(args.train_models, seed=1, budget=args.traj_budget, nt=args.nt, target=args.target,
+                            sigmas=sigmas)
         torch.cuda.synchronize()
         report["trajectories"] = {"models": args.train_models, "samples": int(data["field"].shape[0]),
                                   "seconds": time.perf_counter() - t0,
