@@ -420,7 +420,10 @@ __global__ void __launch_bounds__(FWD_THREADS, 2) fwd_stream_kernel(const __grid
 // bit for bit (sources are injected into halo copies too; receivers are recorded by the tile that
 // holds their first corner). Per step the wavefield crosses HBM once per TB_T steps instead of once
 // per step. The state is read from one set and written to the other (sets alternate per launch),
-// so no CTA overwrites cells a neighbouring CTA still has to read.
+// so no CTA overwrites cells a neighbouring CTA still has to read. Off by default (engine option
+// "temporal_block"): the per-step forward is latency-bound rather than bandwidth-bound, so the
+// saved traffic buys nothing, and the redundant halo updates (31 % of the work) make this kernel
+// slower on the 800 x 300 survey.
 // ------------------------------------------------------------------------------------------------
 constexpr int TB_T = 4;                      // time steps per launch
 constexpr int TB_H = 2 * TB_T;               // halo per side
