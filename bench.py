@@ -128,6 +128,14 @@ def cpu_baseline(start, obs, src, cores: int, sample_models: int):
     return m / dt, dt
 
 
+def gradient_config(models: int, nt: int, checkpoint: int, arith: str = "exact") -> dict:
+    """The gradient workload's `config`, the same for this repository's arm and the reference arm."""
+    return {"workload": f"gradient batch: {models} mixed-family 70x70 models x 5 shots, nt={nt}, dt=1ms, "
+                        f"pml 20, checkpoint every {checkpoint} steps", "models_per_step": models,
+            "shots": SHOTS, "nt": nt, "checkpoint_every": checkpoint,
+            "l2": "inputs larger than L2 (observed 358 MB, checkpoints ~10 GB per step)", "arith": arith}
+
+
 def run_reference(args):
     """The reference's CPU solver path (C++ restatement of geology-core + the engine's adjoint;
     the Rust crate itself cannot be built here) on all host cores."""
@@ -155,10 +163,11 @@ def run_reference(args):
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * tot / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": f"{sample} mixed-family 70x70 models x 5 shots, nt=1000, dt=1ms (bounded sample of the "
-                               f"256-model batch)", "models_per_step": sample},
+        "config": gradient_config(args.models, NT, args.checkpoint),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
-                         "sample": f"{sample} gradients per step, one model per thread"},
+                         "sample": f"each step {sample} of the batch's {args.models} gradients (the first models of "
+                                   f"the same seeded batch), one model per thread; the CPU port keeps every step's "
+                                   f"gradient term in memory instead of checkpointing"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -254,10 +263,8 @@ def run_datagen(args):
         "metric": DATAGEN_METRIC, "value": value, "unit": DATAGEN_UNIT, "n_gpus": 1, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32 (FP16 output)", "data": "synthetic (seeded mixed-family models)",
-        "config": {"workload": f"batched generation: {total} models round-robin over 70x70/100x100/140x140, "
-                               f"5 shots, nt={args.nt}, dt=1ms, low-pass + x4 decimation to FP16, one CUDA graph launch",
-                   "counts": counts, "l2": "inputs and outputs larger than L2 (f32 traces ~8 GB per step)",
-                   "kernels_per_graph": gen.kernels_per_launch},
+        "config": datagen_config(total, args.nt),
+        "launch": {"counts": counts, "kernels_per_graph": gen.kernels_per_launch},
         "e2e": {"value": e2e, "unit": DATAGEN_UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": gen.kernels_per_launch * args.steps, "outputs_finite": ok,
         "per_grid": per_grid,
@@ -406,11 +413,7 @@ def measure_large(nt: int, shots: int, steps: int, warmup: int) -> dict:
         "metric": LARGE_METRIC, "value": value, "unit": LARGE_UNIT, "n_gpus": 1, "steps": steps,
         "warmup": warmup, "ms_per_step": ms / steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded faulted layered model, smoothed start)",
-        "config": {"workload": f"large survey: 800x300 cells at 5 m (padded 844x344), {shots} shots, "
-                               f"800 receivers, dt=0.5ms, nt={nt}, forward + exact adjoint gradient, streamed path",
-                   "checkpointing": "every step's gradient term stored in HBM when it fits (auto)",
-                   "temporal_block": "off (one step per launch); `simulate` also times the engine option",
-                   "l2": "inputs larger than L2 (wavefields ~93 MB + stored terms ~186 GB per gradient)"},
+        "config": large_config(nt, shots),
         "gradients_per_s": steps / (ms / 1000.0),
         "simulate": {f"temporal_block_{tb}": {"ms": t, "gcell_updates_per_s": upd * nt * shots / (t / 1000.0) / 1e9}
                      for tb, t in sim_ms.items()},
@@ -427,6 +430,15 @@ def measure_large(nt: int, shots: int, steps: int, warmup: int) -> dict:
                                       "gcell_updates_per_s": per_launch / (fwd_step_ms / 1000.0) / 1e9}},
         "clocks": summarize_clocks(clk),
     }
+
+
+def large_config(nt: int, shots: int) -> dict:
+    """The large survey's `config`, the same for this repository's arm and the reference arm."""
+    return {"workload": f"large survey: 800x300 cells at 5 m (padded 844x344), {shots} shots, 800 receivers, "
+                        f"dt=0.5ms, nt={nt}, forward + exact adjoint gradient, streamed path",
+            "checkpointing": "every step's gradient term stored in HBM when it fits (auto)",
+            "temporal_block": "off (one step per launch); `simulate` also times the engine option",
+            "l2": "inputs larger than L2 (wavefields ~93 MB + stored terms ~186 GB per gradient)"}
 
 
 def run_large(args):
@@ -477,9 +489,9 @@ def run_reference_large(args):
     print(json.dumps({"impl": "reference", "metric": LARGE_METRIC, "value": value, "unit": LARGE_UNIT,
                       "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": None,
                       "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-                      "data": "synthetic", "config": {"workload": sample},
+                      "data": "synthetic", "config": large_config(args.nt, args.shots),
                       "cpu_baseline": {"value": value, "unit": LARGE_UNIT, "cores": cores, "kind": "port",
-                                       "sample": sample},
+                                       "sample": f"each step {sample}"},
                       "e2e": {"value": value, "unit": LARGE_UNIT, "h2d_bytes_per_step": 0,
                               "d2h_bytes_per_step": 0}}), flush=True)
     return 0
@@ -567,6 +579,13 @@ def run_train(args):
     return 0
 
 
+def datagen_config(models: int, nt: int) -> dict:
+    """The generation workload's `config`, the same for this repository's arm and the reference arm."""
+    return {"workload": f"batched generation: {models} models round-robin over 70x70/100x100/140x140, 5 shots, "
+                        f"nt={nt}, dt=1ms, low-pass + x4 decimation to FP16, one CUDA graph launch",
+            "l2": "inputs and outputs larger than L2 (f32 traces ~8 GB per step)"}
+
+
 def run_reference_datagen(args):
     """The reference's CPU forward (C++ restatement) on a bounded sample of the generation mix."""
     from oracle import native as o
@@ -588,9 +607,10 @@ def run_reference_datagen(args):
                       "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
                       "ms_per_step": 1000.0 * sum(times) / len(times), "higher_is_better": True, "scaling": "weak",
                       "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-                      "config": {"workload": f"{m} models of the 70/100/140 mix (bounded sample), forward only"},
+                      "config": datagen_config(args.models, args.nt),
                       "cpu_baseline": {"value": value, "unit": DATAGEN_UNIT, "cores": cores, "kind": "port",
-                                       "sample": f"{m} models per step"},
+                                       "sample": f"each step {m} models of the same mix, forward in f32 without the "
+                                                 f"FP16 decimation, one shot per thread"},
                       "e2e": {"value": value, "unit": DATAGEN_UNIT, "h2d_bytes_per_step": 0,
                               "d2h_bytes_per_step": 0}}), flush=True)
     return 0
@@ -809,13 +829,9 @@ def main():
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded mixed-family models: flat, curved, faulted, blob inclusions)",
-        "config": {"workload": f"gradient batch: {M} mixed-family 70x70 models x 5 shots, nt={nt}, dt=1ms, "
-                               f"pml 20, checkpoint every {args.checkpoint} steps", "models_per_step": M,
-                   "shots": SHOTS, "nt": nt, "checkpoint_every": args.checkpoint,
-                   "l2": "inputs larger than L2 (observed 358 MB, checkpoints ~10 GB per step)",
-                   "launch_shape": {"forward": eng.launch_shape("forward"), "adjoint": eng.launch_shape("adjoint")},
-                   "autotuned": tuned is not None,
-                   "arith": args.arith},
+        "config": gradient_config(M, nt, args.checkpoint, args.arith),
+        "launch": {"shape": {"forward": eng.launch_shape("forward"), "adjoint": eng.launch_shape("adjoint")},
+                   "autotuned": tuned is not None},
         "gcell_updates_per_s": cells_per_s / 1e9,
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": launches,
