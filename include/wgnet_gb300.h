@@ -86,6 +86,14 @@ int wg_evaluate_adjoint_dev(wg_engine* eng, const float* d_vel_mps, const float*
  * out), with the message in wg_last_error(). The host-pointer entry points check it themselves. */
 int wg_engine_status(wg_engine* eng, void* stream);
 
+/* Self-test of the time-out path that wg_engine_status reports: clears the engine's status word
+ * and launches, on `stream`, one CTA whose bounded mbarrier wait (the wait the streamed kernels use
+ * for their TMA copies) waits for a copy that is never issued. The wait gives up after `polls`
+ * polls (1 .. 2^22; the kernels use 2^22), records the error and the kernel returns: no fault, no
+ * hang, the context stays usable. wg_engine_status then returns WG_ERR_CUDA. No reference
+ * counterpart. */
+int wg_selftest_wait_timeout(wg_engine* eng, long long polls, void* stream);
+
 /* Wavefield checkpoint interval for evaluate_adjoint: snapshots every k steps, segments recomputed
  * in reverse. k >= nt stores the gradient term of every step (the reference's scheme,
  * wave_wgpu.rs:181-182); so does k <= 0 on the resident path, while on the streamed path k <= 0

@@ -10,6 +10,9 @@ device-pointer entry points. GPU tests, through the C ABI.
   crates/wave-gauss-rs/src/wave_wgpu.rs:853) through the device entry points too: `WaveLoss.apply`,
   `evaluate_adjoint_torch` and the allocation-free entry point (status read with
   wg_engine_status), and a later good call on the same engine succeeds (the word is cleared per call).
+* A bounded wait that runs out: the streamed kernels' mbarrier wait on a copy that is never issued
+  gives up after its poll limit and the kernel records the error instead of hanging; the status
+  reads WG_ERR_CUDA, and the same context then computes the same traces and gradient as before.
 """
 
 from __future__ import annotations
@@ -105,3 +108,28 @@ def test_zero_energy_raises_through_the_device_entry_points(cuda_lib):
                                                grad.data_ptr(), stream))
     assert lib.wg_engine_status(eng._h, stream) == _lib.WG_OK
     np.testing.assert_array_equal(grad.cpu().numpy(), g2.cpu().numpy())
+
+
+def test_a_bounded_wait_that_runs_out_reports_and_the_context_stays_usable(cuda_lib):
+    import torch
+
+    from wgnet_gb300 import _lib
+
+    eng = _engine_1ms(shots=2, nt=200)
+    lib = _lib.load()
+    stream = torch.cuda.current_stream().cuda_stream
+    vel = torch.tensor(layered_model(5), device="cuda")[None].contiguous()
+    before = eng.simulate_torch(vel)
+    obs = eng.simulate_torch(vel * 1.05)
+    loss0, grad0 = eng.evaluate_adjoint_torch(vel, obs)
+    assert lib.wg_selftest_wait_timeout(eng._h, 0, stream) == _lib.WG_ERR_ARG
+    assert lib.wg_selftest_wait_timeout(eng._h, (1 << 22) + 1, stream) == _lib.WG_ERR_ARG
+    _lib.check(lib.wg_selftest_wait_timeout(eng._h, 1 << 14, stream))
+    assert lib.wg_engine_status(eng._h, stream) == _lib.WG_ERR_CUDA
+    assert "timed out" in _lib.last_error()
+    # the context is intact: the next calls clear the word and compute the same results as before
+    after = eng.simulate_torch(vel)
+    assert lib.wg_engine_status(eng._h, stream) == _lib.WG_OK
+    assert torch.equal(after, before)
+    loss1, grad1 = eng.evaluate_adjoint_torch(vel, obs)
+    assert torch.equal(loss1, loss0) and torch.equal(grad1, grad0)

@@ -49,6 +49,7 @@ SIGNATURES: dict[str, tuple] = {
     "wg_evaluate_adjoint": (_I, [_P, _P, _P, _I, _P, _P]),
     "wg_evaluate_adjoint_dev": (_I, [_P, _P, _P, _I, _P, _P, _P]),
     "wg_engine_status": (_I, [_P, _P]),
+    "wg_selftest_wait_timeout": (_I, [_P, ctypes.c_longlong, _P]),
     "wg_set_checkpoint_interval": (_I, [_P, _I]),
     "wg_get_checkpoint_interval": (_I, [_P]),
     "wg_set_option": (_I, [_P, ctypes.c_char_p, _I]),

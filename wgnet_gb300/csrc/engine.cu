@@ -822,6 +822,16 @@ int wg_engine_status(wg_engine* e, void* stream) {
   return WG_OK;
 }
 
+int wg_selftest_wait_timeout(wg_engine* e, long long polls, void* stream) {
+  if (!e) return fail(WG_ERR_ARG, "null engine");
+  if (polls < 1 || polls > (1LL << 22)) return fail(WG_ERR_ARG, "polls must be in [1, 2^22]");
+  std::lock_guard<std::mutex> lk(e->mu);
+  WG_CK(cudaSetDevice(e->device));
+  cudaStream_t st = pick_stream(e, stream);
+  WG_CK(cudaMemsetAsync(e->d_status.p, 0, sizeof(int), st));
+  return wg::wait_timeout_selftest(static_cast<int*>(e->d_status.p), polls, st);
+}
+
 int wg_evaluate_adjoint(wg_engine* e, const float* vel, const float* obs, int models, double* loss, float* grad) {
   if (!e || !vel || !obs || !loss || !grad) return fail(WG_ERR_ARG, "null argument");
   if (models < 1) return fail(WG_ERR_ARG, "models must be >= 1");

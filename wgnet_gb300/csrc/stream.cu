@@ -83,10 +83,10 @@ __device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, unsigned bytes) {
   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
 }
 
-// Bounded wait for the phase with parity `parity`; false when the limit is reached.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity) {
+// Bounded wait for the phase with parity `parity`; false when `limit` polls are reached.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity, long limit = kWaitLimit) {
   const unsigned a = smem_u32(bar);
-  for (long i = 0; i < kWaitLimit; ++i) {
+  for (long i = 0; i < limit; ++i) {
     unsigned ok;
     asm volatile(
         "{\n\t.reg .pred p;\n\t"
@@ -1047,7 +1047,27 @@ int make_fwd_maps(FwdMaps* m, const float* W, const float* vel, int nx, int nz, 
 
 constexpr size_t kAdjSmem = (7 * BZ * BX) * 4 + 16 + 128;
 
+// Self-test of the time-out path: the kernels' bounded wait on an mbarrier that expects 16 bytes
+// of a copy that is never issued. The wait gives up after `polls` polls, the CTA records ST_CUDA
+// in `status` and the kernel returns (no copy is in flight, so there is nothing to drain).
+__global__ void wait_timeout_probe_kernel(int* status, long polls) {
+  __shared__ __align__(8) uint64_t bar;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) mbar_expect_tx(&bar, 16);  // the arrival; the 16 bytes never land
+  __syncthreads();
+  if (__syncthreads_or(mbar_wait(&bar, 0, polls) ? 0 : 1) && threadIdx.x == 0) report(status);
+}
+
 }  // namespace
+
+int wait_timeout_selftest(int* d_status, long long polls, cudaStream_t st) {
+  wait_timeout_probe_kernel<<<1, 64, 0, st>>>(d_status, static_cast<long>(polls));
+  return cudaGetLastError() == cudaSuccess ? WG_OK : report_error(WG_ERR_CUDA, "wait self-test launch failed");
+}
 
 struct StreamWork {
   Buf vpad, mask, traces, energy, scale, stored, ckpt, gacc;

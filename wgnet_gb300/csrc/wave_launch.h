@@ -107,6 +107,10 @@ int stream_simulate(StreamWork* w, const EngineView& v, const int* h_rec_cell, c
 int stream_gradient(StreamWork* w, const EngineView& v, const int* h_rec_cell, const float* d_vis, const float* d_obs,
                     int models, double* d_loss, float* d_grad, cudaStream_t st, const StreamTimer& timer);
 
+// Launch the bounded-wait self-test (stream.cu): one CTA's wait on an mbarrier nothing completes
+// gives up after `polls` polls and records ST_CUDA in *d_status.
+int wait_timeout_selftest(int* d_status, long long polls, cudaStream_t st);
+
 // out[i] = in[i] * alpha (unit conversion), n elements.
 cudaError_t launch_scale(const float* in, float alpha, size_t n, float* out, cudaStream_t s);
 
