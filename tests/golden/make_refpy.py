@@ -1,6 +1,6 @@
 """Generate fixtures by running the reference's own Python layer (python/wgnet/data.py, physics.py,
-render.py, refine.py) unchanged, with `import wave_gauss_rs` resolving to the oracle-backed
-restatement of the PyO3 module (oracle/pyo3_standin.py).
+render.py, refine.py, fwi_eval.py) unchanged, with `import wave_gauss_rs` resolving to the
+oracle-backed restatement of the PyO3 module (oracle/pyo3_standin.py).
 
     python tests/golden/make_refpy.py /path/to/WGNet
 
@@ -8,7 +8,8 @@ The reference's Python cannot run where the GPU tests run (it is not part of thi
 its outputs on fixed inputs are stored here (refpy.npz) and tests/test_gpu_refpy.py runs this
 repository's WavePhysics and refine() on the same inputs through the CUDA engine. Cases follow
 python/verify.py: the adjoint through the renderer (57-74, 2 shots, nt 501), the band identity
-(76-84) and budgeted refinement (107-117, 2 shots, nt 801, 30 solves, bands 10 Hz / full).
+(76-84) and budgeted refinement (107-117, 2 shots, nt 801, 30 solves, bands 10 Hz / full); and
+fwi_eval.py's budgeted pixel-grid FWI (32-57, 2 shots, nt 501, 12 solves, bands 8 Hz / full).
 """
 
 from __future__ import annotations
@@ -35,7 +36,7 @@ def load_reference(ref_root: Path) -> dict:
     pkg.__path__ = [str(pkg_dir)]
     sys.modules["wgnet"] = pkg
     mods = {}
-    for name in ("data", "render", "physics", "refine"):
+    for name in ("data", "render", "physics", "refine", "igm", "model", "train", "fwi_eval"):
         spec = importlib.util.spec_from_file_location(f"wgnet.{name}", pkg_dir / f"{name}.py")
         mod = importlib.util.module_from_spec(spec)
         sys.modules[f"wgnet.{name}"] = mod
@@ -114,7 +115,26 @@ def main() -> None:
                ref_hist_solves=np.array([h["solves"] for h in hist], np.int64),
                ref_hist_accepted=np.array([h["accepted"] for h in hist], bool),
                ref_hist_band=np.array([-1.0 if h["band_hz"] is None else h["band_hz"] for h in hist], np.float64))
+    # budgeted pixel-grid FWI (fwi_eval.py:32-57) from a smoothed start
+    from scipy.ndimage import gaussian_filter
+
+    physics = physics_mod.WavePhysics(shots=2, nt=501)
+    gen = torch.Generator().manual_seed(6)
+    with torch.no_grad():
+        truth = (torch.full((1, 70, 70), 2.5) + render.render_residual(random_scene(render, gen, 10)))[0].numpy()
+    start = gaussian_filter(truth, 4.0, mode="nearest").astype(np.float32)
+    observed = physics.simulate(truth[None])[0]
+    final, fhist = m["fwi_eval"].fwi(start, observed, physics, [8.0, None], 12, 1.5)
+    physics.set_band(8.0)
+    out["fwi_band8_wavelet"] = physics.engine.wavelet()
+    out["fwi_band8_observed"] = physics.bandlimit(observed)
+    physics.set_band(None)
+    out.update(fwi_truth=truth, fwi_start=start, fwi_observed=observed, fwi_final=final,
+               fwi_hist_misfit=np.array([h["misfit"] for h in fhist], np.float64),
+               fwi_hist_solves=np.array([h["solves"] for h in fhist], np.int64))
     np.savez_compressed(HERE / "refpy.npz", **out)
+    print(f"fwi: MAE {np.abs(start - truth).mean() * 1000:.1f} -> {np.abs(final - truth).mean() * 1000:.1f} m/s, "
+          f"history {fhist}")
     print(f"refine: {res.initial_loss:.4e} -> {res.final_loss:.4e} in {res.solves} solves, "
           f"{len(hist)} iterations; loss_and_grad {losses}")
 
