@@ -133,7 +133,9 @@ def gradient_config(models: int, nt: int, checkpoint: int, arith: str = "exact")
     return {"workload": f"gradient batch: {models} mixed-family 70x70 models x 5 shots, nt={nt}, dt=1ms, "
                         f"pml 20, checkpoint every {checkpoint} steps", "models_per_step": models,
             "shots": SHOTS, "nt": nt, "checkpoint_every": checkpoint,
-            "l2": "inputs larger than L2 (observed 358 MB, checkpoints ~10 GB per step)", "arith": arith}
+            "l2": "inputs larger than L2 (observed 358 MB, checkpoints ~10 GB per step)", "arith": arith,
+            "passband": "full band (a 6/9/12/15 Hz passband changes the wavelet and the observed data, not the work of "
+                        "a gradient)"}
 
 
 def run_reference(args):
