@@ -346,3 +346,42 @@ def test_every_shape_gradient_bitexact_other_grids(cuda_lib, nxv, nzv):
         eng.set_launch_shape("forward", shape)
         loss, grad = eng.evaluate_adjoint(cur, obs)
         np.testing.assert_array_equal(grad, rg, err_msg=f"forward shape {shape}")
+
+
+def test_non_finite_inputs_follow_the_reference(cuda_lib):
+    """Velocities go through Rust's f32::clamp (wave_wgpu.rs:714-734): a NaN cell stays NaN and
+    spreads through the wavefield, +-inf cells clamp to vmax / vmin with a zero clamp mask (no
+    gradient there); observed data whose energy is NaN fail the reference's `energy > 0` check
+    (wave_wgpu.rs:853), like zero energy. Traces and gradients equal the oracle's, NaNs included."""
+    sv, vel, src = small_case(seed=8, shots=2, nt=120)
+    eng = make_engine(sv, src, checkpoint_every=40)
+    wav = eng.wavelet()
+    inf = vel.copy()
+    inf[5, 7], inf[9, 2] = np.inf, -np.inf
+    nan = vel.copy()
+    nan[6, 10] = np.nan
+    models = np.stack([inf, nan])
+    got = eng.simulate(models)
+    ref = o.forward(sv, models, src, wav)
+    np.testing.assert_array_equal(got, ref)
+    assert np.isfinite(got[0]).all() and np.isnan(got[1]).any()
+    obs = o.forward(sv, np.stack([vel, vel]) * np.float32(1.02), src, wav)
+    loss, grad = eng.evaluate_adjoint(models, obs)
+    rl, rg = o.evaluate_adjoint(sv, models, src, wav, obs)
+    np.testing.assert_array_equal(grad, rg)
+    np.testing.assert_array_equal(loss, rl)
+    assert grad[0, 5, 7] == 0.0 and grad[0, 9, 2] == 0.0 and np.isfinite(grad[0]).all()
+    bad = obs.copy()
+    bad[0, 0, 3, 4] = np.nan
+    with pytest.raises(RuntimeError, match="zero energy"):
+        eng.evaluate_adjoint(np.stack([vel, vel]), bad)
+
+
+def test_empty_batch_is_an_argument_error(cuda_lib):
+    sv, vel, src = small_case(seed=9, shots=2, nt=60)
+    eng = make_engine(sv, src)
+    empty = np.zeros((0, sv.nz_vis, sv.nx_vis), np.float32)
+    with pytest.raises(ValueError):
+        eng.simulate(empty)
+    with pytest.raises(ValueError):
+        eng.evaluate_adjoint(empty, np.zeros((0, sv.shots, sv.nt, sv.n_receivers), np.float32))
