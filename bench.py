@@ -128,6 +128,21 @@ def cpu_baseline(start, obs, src, cores: int, sample_models: int):
     return m / dt, dt
 
 
+def learned_refinement_brief(models: int = 32) -> dict:
+    """Learned-plus-exact refinement against plain projected L-BFGS, the solve-count half of the
+    metric: `models` held-out seeded 70x70 models, 5 shots, budget 160 solves, bands 6 / 9 / 12 Hz /
+    full, from a 5-cell and from an 8-cell smoothed start, with the committed update network."""
+    from wgnet_gb300.learned import evaluate
+    from wgnet_gb300.precond import UpdateNet
+
+    net = UpdateNet.load(Path(__file__).resolve().parent / "wgnet_gb300" / "weights" / "update_net.npz")
+    out = {}
+    for sigma, seed in ((5.0, 777), (8.0, 888)):
+        r = evaluate(net, models, seed=seed, shots=5, budget=160, sigma=sigma)
+        out[f"start_smoothed_{int(sigma)}_cells"] = {k: v for k, v in r.items() if k != "per_model"}
+    return out
+
+
 def gradient_config(models: int, nt: int, checkpoint: int, arith: str = "exact") -> dict:
     """The gradient workload's `config`, the same for this repository's arm and the reference arm."""
     return {"workload": f"gradient batch: {models} mixed-family 70x70 models x 5 shots, nt={nt}, dt=1ms, "
@@ -686,6 +701,8 @@ def main():
     ap.add_argument("--no-autotune", action="store_true", help="keep the engine's default launch shapes")
     ap.add_argument("--no-large", action="store_true",
                     help="skip the short measurement of the 800x300 streamed survey in the default run")
+    ap.add_argument("--no-learned", action="store_true",
+                    help="skip the short learned-versus-plain refinement comparison in the default run")
     ap.add_argument("--no-fast", action="store_true",
                     help="skip the secondary measurement with the fast-arithmetic forward (arith 1)")
     ap.add_argument("--arith", default="exact", choices=["exact", "fast"],
@@ -870,6 +887,8 @@ def main():
         del d_obs, d_start, d_true, h_obs
         torch.cuda.empty_cache()
         line["large_survey"] = measure_large(4000, 40, steps=2, warmup=1)
+    if not args.no_learned and rank == 0 and world == 1:
+        line["learned_refinement"] = learned_refinement_brief()
     if rank == 0:
         print(json.dumps(line), flush=True)
     if dist:
