@@ -385,3 +385,28 @@ def test_empty_batch_is_an_argument_error(cuda_lib):
         eng.simulate(empty)
     with pytest.raises(ValueError):
         eng.evaluate_adjoint(empty, np.zeros((0, sv.shots, sv.nt, sv.n_receivers), np.float32))
+
+
+def test_reference_default_engine_through_the_dropin_module(cuda_lib):
+    """The reference's own engine configuration: `PyWaveEngine()` with its defaults (5 shots,
+    nt 2001, dt 0.5 ms, 15 Hz, pml 20; lib.rs:51-72, data.py:32-33) through the drop-in module,
+    with its default sources and every surface receiver: traces, loss and gradient equal the
+    oracle's bit for bit."""
+    import wave_gauss_rs
+
+    e = wave_gauss_rs.PyWaveEngine()
+    assert (e.shots, e.nt, e.nrec) == (5, 2001, 70)
+    sv = o.Survey()  # the same defaults
+    src = e.sources()
+    wav = e.wavelet()
+    np.testing.assert_array_equal(wav, o.ricker(sv.nt, sv.dt, sv.peak_hz))
+    true = layered_model(21)
+    cur = layered_model(22)
+    tr = e.simulate(true.reshape(-1))
+    ref = o.forward(sv, true, src, wav)[0]
+    np.testing.assert_array_equal(tr, ref)
+    loss, grad = e.evaluate_adjoint(cur.reshape(-1), tr.reshape(-1))
+    rl, rg = o.evaluate_adjoint(sv, cur, src, wav, ref[None])
+    np.testing.assert_array_equal(grad, rg[0])
+    # the engine returns the loss as f32 (wave_wgpu.rs:965-985: the f64 sum rounded once)
+    assert isinstance(loss, float) and loss == float(np.float32(rl[0]))
