@@ -128,6 +128,61 @@ def cpu_baseline(start, obs, src, cores: int, sample_models: int):
     return m / dt, dt
 
 
+# One renderer evaluation (render.py:86-109): 2 subtractions, the rotation (4 mul, 2 add), the
+# scales (2 mul), u^2 + v^2 (2 mul, 1 add), the -1/2 (1 mul) and the accumulation (1 mul, 1 add),
+# plus one exp (an ex2 on the SFU)
+RENDER_FLOPS_PER_EVAL = 17
+SFU_EX2_PER_SM_CLOCK = 16
+
+
+def renderer_rate(sms: int, sm_mhz: float, batch: int = MODELS, reps: int = 20) -> dict:
+    """The Gaussian renderer on the gradient workload's batch (`batch` models x 1225 slots, 25 x 25
+    windows): forward, and forward + backward, timed with CUDA events. Evaluations are the in-grid
+    window pixels (the reference also evaluates the out-of-grid ones, on a spare pixel); each costs
+    RENDER_FLOPS_PER_EVAL FP32 operations and one exp, so both the FP32 pipe and the SFU bound it."""
+    import torch
+
+    from wgnet_gb300 import _lib
+    from wgnet_gb300 import render as R
+
+    gen = torch.Generator().manual_seed(1)
+    raw = torch.randn(batch, R.N_SLOTS, 6, generator=gen) * 0.5
+    raw[..., 5] = torch.randn(batch, R.N_SLOTS, generator=gen) * 1.5
+    params = R.activate_gaussians(raw).cuda().contiguous().requires_grad_(True)
+    cot = torch.randn(batch, R.GRID, R.GRID, device="cuda")
+    for _ in range(3):
+        torch.autograd.grad(R.render_residual(params), params, cot)
+    torch.cuda.synchronize()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+    _lib.launch_count(reset=True)
+    with torch.no_grad():
+        ev[0].record()
+        for _ in range(reps):
+            R.render_residual(params)
+        ev[1].record()
+    for _ in range(reps):
+        torch.autograd.grad(R.render_residual(params), params, cot)
+    ev[2].record()
+    torch.cuda.synchronize()
+    launches = _lib.launch_count()
+    fwd_ms = ev[0].elapsed_time(ev[1]) / reps
+    both_ms = ev[1].elapsed_time(ev[2]) / reps
+    evals = float(R.slot_windows()[2].sum()) * batch
+    fp32_peak = sms * FP32_LANES_PER_SM * 2 * sm_mhz * 1e6 / 1e12
+    sfu_peak = sms * SFU_EX2_PER_SM_CLOCK * sm_mhz * 1e6
+    achieved = evals * RENDER_FLOPS_PER_EVAL / (fwd_ms / 1000.0) / 1e12
+    return {"batch": batch, "evaluations_per_forward": evals,
+            "evaluations_reference_counts": float(batch * R.N_SLOTS * R.WIN_SIDE * R.WIN_SIDE),
+            "forward_ms": fwd_ms, "forward_backward_ms": both_ms, "launches_per_rep": launches / (2 * reps),
+            "roofline": {"kernel": "render_fwd", "bound": "fp32", "achieved": achieved, "peak": fp32_peak,
+                         "unit": "TFLOP/s", "frac": achieved / fp32_peak,
+                         "flops_per_evaluation": RENDER_FLOPS_PER_EVAL,
+                         "sfu": {"achieved_exp_per_s": evals / (fwd_ms / 1000.0), "peak": sfu_peak,
+                                 "frac": evals / (fwd_ms / 1000.0) / sfu_peak,
+                                 "peak_source": f"computed: {sms} SMs x {SFU_EX2_PER_SM_CLOCK} ex2 per clock x "
+                                                f"{sm_mhz:.0f} MHz"}}}
+
+
 def learned_refinement_brief(models: int = 32) -> dict:
     """Learned-plus-exact refinement against plain projected L-BFGS, the solve-count half of the
     metric: `models` held-out seeded 70x70 models, 5 shots, budget 160 solves, bands 6 / 9 / 12 Hz /
@@ -870,6 +925,8 @@ def main():
                      "ncu_small_case": NCU_SMALL_CASE.get(names[dom])},
     }
     line["clocks"] = clocks
+    if rank == 0:
+        line["renderer"] = renderer_rate(props.multi_processor_count, sm_mhz)
     if args.arith == "exact" and not args.no_fast:
         line["fast_arith"] = fast_arith_rate(args, eng, lib, d_start, d_obs, h_vel, h_obs, h_loss, h_grad, M, dist,
                                              dev, world, tuned is not None)
