@@ -3,7 +3,8 @@
 //
 // Forward gathers: each pixel sums the slots whose window covers it, in increasing slot order (the
 // order in which index_add_ accumulates on the CPU), from per-slot constants staged in shared
-// memory. Backward: one warp per slot reduces the six parameter gradients over its window.
+// memory; one thread computes a 2 x 2 pixel quad, so each slot's constants serve up to four pixels.
+// Backward: one warp per slot reduces the six parameter gradients over its window.
 #include <cuda_runtime.h>
 
 #include "wave_launch.h"
@@ -33,7 +34,15 @@ __device__ __forceinline__ SlotC slot_consts(const float* p, int i) {
   return k;
 }
 
-__global__ void __launch_bounds__(512) render_fwd_kernel(const float* __restrict__ params, float* __restrict__ field) {
+// One thread per 2 x 2 pixel quad (2n..2n+1, 2m..2m+1): row 2n is covered by the slots
+// iz in [n-6, n+6], row 2n+1 by [n-5, n+6] (and the same for the columns), so each slot's
+// constants, loaded once, serve up to four pixels. Every pixel still sums its slots in increasing
+// slot order. Blocks (QBLK threads, blockIdx.y) split a model's 1225 quads; each block stages all
+// slot constants of its model (blockIdx.x).
+constexpr int QBLK = 256;
+constexpr int QBLOCKS = (SLOTS + QBLK - 1) / QBLK;
+
+__global__ void __launch_bounds__(QBLK) render_fwd_kernel(const float* __restrict__ params, float* __restrict__ field) {
   __shared__ float sh[7 * SLOTS];
   const int b = blockIdx.x;
   const float* pb = params + static_cast<size_t>(b) * SLOTS * NPAR;
@@ -48,24 +57,38 @@ __global__ void __launch_bounds__(512) render_fwd_kernel(const float* __restrict
     sh[6 * SLOTS + i] = k.w;
   }
   __syncthreads();
-  for (int p = threadIdx.x; p < GRID * GRID; p += blockDim.x) {
-    const int pz = p / GRID, px = p % GRID;
-    // slot (iz, ix) covers pixel (pz, px) when |pz - 2 iz| <= WIN and |px - 2 ix| <= WIN
-    const int iz0 = max(0, (pz - WIN + 1) / 2), iz1 = min(SIDE - 1, (pz + WIN) / 2);
-    const int ix0 = max(0, (px - WIN + 1) / 2), ix1 = min(SIDE - 1, (px + WIN) / 2);
-    const float fx = static_cast<float>(px) + 0.5f, fz = static_cast<float>(pz) + 0.5f;
-    float acc = 0.0f;
-    for (int iz = iz0; iz <= iz1; ++iz)
-      for (int ix = ix0; ix <= ix1; ++ix) {
-        const int i = iz * SIDE + ix;
-        const float dx = fx - sh[i], dz = fz - sh[SLOTS + i];
-        const float c = sh[4 * SLOTS + i], s = sh[5 * SLOTS + i];
-        const float u = (dx * c + dz * s) * sh[2 * SLOTS + i];
-        const float v = (dz * c - dx * s) * sh[3 * SLOTS + i];
-        acc += sh[6 * SLOTS + i] * expf(-0.5f * (u * u + v * v));
+  const int q = blockIdx.y * QBLK + threadIdx.x;
+  if (q >= SLOTS) return;
+  const int n = q / SIDE, m = q % SIDE;
+  const int iz0 = max(0, n - WIN / 2), iz1 = min(SIDE - 1, n + WIN / 2);
+  const int ix0 = max(0, m - WIN / 2), ix1 = min(SIDE - 1, m + WIN / 2);
+  const float fx0 = static_cast<float>(2 * m) + 0.5f, fx1 = static_cast<float>(2 * m + 1) + 0.5f;
+  const float fz0 = static_cast<float>(2 * n) + 0.5f, fz1 = static_cast<float>(2 * n + 1) + 0.5f;
+  float a00 = 0.0f, a01 = 0.0f, a10 = 0.0f, a11 = 0.0f;  // a[row][col]
+  auto term = [](float fx, float fz, float cx, float cz, float c, float s, float isx, float isz, float w) {
+    const float dx = fx - cx, dz = fz - cz;
+    const float u = (dx * c + dz * s) * isx;
+    const float v = (dz * c - dx * s) * isz;
+    return w * expf(-0.5f * (u * u + v * v));
+  };
+  for (int iz = iz0; iz <= iz1; ++iz) {
+    const bool row1 = iz >= n - WIN / 2 + 1;  // slot row iz also covers pixel row 2n + 1
+    for (int ix = ix0; ix <= ix1; ++ix) {
+      const bool col1 = ix >= m - WIN / 2 + 1;
+      const int i = iz * SIDE + ix;
+      const float cx = sh[i], cz = sh[SLOTS + i], isx = sh[2 * SLOTS + i], isz = sh[3 * SLOTS + i];
+      const float c = sh[4 * SLOTS + i], s = sh[5 * SLOTS + i], w = sh[6 * SLOTS + i];
+      a00 += term(fx0, fz0, cx, cz, c, s, isx, isz, w);
+      if (col1) a01 += term(fx1, fz0, cx, cz, c, s, isx, isz, w);
+      if (row1) {
+        a10 += term(fx0, fz1, cx, cz, c, s, isx, isz, w);
+        if (col1) a11 += term(fx1, fz1, cx, cz, c, s, isx, isz, w);
       }
-    field[static_cast<size_t>(b) * GRID * GRID + p] = acc;
+    }
   }
+  float* f = field + static_cast<size_t>(b) * GRID * GRID + (2 * n) * GRID + 2 * m;
+  *reinterpret_cast<float2*>(f) = make_float2(a00, a01);
+  *reinterpret_cast<float2*>(f + GRID) = make_float2(a10, a11);
 }
 
 __global__ void __launch_bounds__(256) render_bwd_kernel(const float* __restrict__ params, const float* __restrict__ cot,
@@ -123,7 +146,7 @@ __global__ void __launch_bounds__(256) render_bwd_kernel(const float* __restrict
 extern "C" int wg_render_fwd_dev(const float* d_params, int batch, float* d_field, void* stream) {
   if (batch < 0 || (batch > 0 && (!d_params || !d_field))) return wg::report_error(WG_ERR_ARG, "bad render arguments");
   if (batch == 0) return WG_OK;
-  render_fwd_kernel<<<batch, 512, 0, static_cast<cudaStream_t>(stream)>>>(d_params, d_field);
+  render_fwd_kernel<<<dim3(batch, QBLOCKS), QBLK, 0, static_cast<cudaStream_t>(stream)>>>(d_params, d_field);
   wg::note_launch();
   const cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? WG_OK : wg::report_error(WG_ERR_CUDA, cudaGetErrorString(e));
